@@ -1,0 +1,40 @@
+"""Loading of the golden fixtures (produced by tests/golden/make_golden.py from the reference)."""
+import ast
+import os
+
+import numpy as np
+
+from bes_gb300 import meshgen
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+MESHES = {
+    "bump_channel_12x4x4_h0.04": lambda: meshgen.bump_channel(12, 4, 4, 0.04),
+    "bump_channel_12x4x4_h0.08": lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+    "gaussian_box_8x4x8_r1.05": lambda: meshgen.gaussian_box(8, 4, 8),
+}
+
+CASES = ["explicit_bump_local", "explicit_bump_global", "explicit_gauss_pitch",
+         "explicit_bump_supersonic", "implicit_bump_jacobi", "implicit_bump_ilu0"]
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    data = {k: z[k] for k in z.files}
+    info = ast.literal_eval(str(data.pop("meta")))
+    return data, info
+
+
+def mesh_of(info):
+    return MESHES[info["mesh"]]()
+
+
+def oracle_kwargs(info):
+    m = info["meta"]
+    kw = dict(solver=0 if m["solver"] == "EXPLICIT" else 1,
+              local_dt=1 if m["local"] == "YES" else 0, cfl=m["cfl"], mach=tuple(m["mach"]))
+    if m["solver"] == "IMPLICIT":
+        kw.update(cfl_max=m["cfl_max"], cfl_exp=(1.0, 1.0),
+                  lin_precond=1 if m["smoother"] == "ILU0" else 0, lin_tol=m["lin_tol"],
+                  lin_maxiter=m["lin_maxiter"], lin_restart=30)
+    return kw

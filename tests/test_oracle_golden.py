@@ -1,0 +1,111 @@
+"""The CPU restatement (oracle/) against golden data produced by the reference itself.
+
+These pin the oracle: every GPU parity test trusts it only because these pass.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from tests import _golden as G
+
+TOL = 1e-12  # relative; the restatement follows the reference's operation order
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    scale = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() / scale
+
+
+@pytest.mark.parametrize("case", G.CASES)
+def test_geometry_matches_reference(case):
+    ref, info = G.load(case)
+    if "geo_volume" not in ref:
+        pytest.skip("no geometry dump for this case")
+    O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
+    geo = O.geometry()
+    for k in ("volume", "centroid", "vec_to_face", "weight", "face_S", "face_n", "face_area",
+              "face_center"):
+        assert rel_err(geo[k], ref["geo_" + k]) <= 1e-14, k
+    for k in ("cell_face", "cell_adj", "face_owner", "face_neigh", "face_type", "muscl_slot"):
+        assert np.array_equal(geo[k].ravel(), ref["geo_" + k]), k
+
+
+@pytest.mark.parametrize("case", [c for c in G.CASES if c.startswith("explicit")])
+def test_explicit_history_matches_reference(case):
+    ref, info = G.load(case)
+    O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
+    hist = O.explicit_run(info["steps"])
+    refh = ref["residual_history"].reshape(-1, 10)
+    # per-iteration L2 and max norm of R of the last stage, per variable
+    assert np.max(np.abs(hist - refh) / np.maximum(np.abs(refh), 1e-300)) <= TOL
+    assert rel_err(O.get_state(), ref["final_state"]) <= TOL
+
+
+@pytest.mark.parametrize("case", [c for c in G.CASES if c.startswith("explicit")])
+def test_explicit_operators_match_reference(case):
+    ref, info = G.load(case)
+    if "op_state" not in ref:
+        pytest.skip("no operator dump")
+    O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
+    O.set_state(ref["op_state"])
+    ops = O.operators(info["meta"]["cfl"])
+    assert rel_err(ops["dt"], ref["op_dt"]) <= TOL
+    assert rel_err(ops["grad"], ref["op_grad"]) <= TOL
+    assert rel_err(ops["limiter"], ref["op_limiter"]) <= TOL
+    assert rel_err(ops["face_UL"], ref["op_face_UL"]) <= TOL
+    assert rel_err(ops["face_UR"], ref["op_face_UR"]) <= TOL
+    assert rel_err(ops["face_flux"], ref["op_face_flux"]) <= TOL
+
+
+def _scalar_csr_vals(asm, nc):
+    """Oracle block CSR -> the reference's scalar CSR value order (row c*5+r: blocks in
+    pattern order, 5 columns each)."""
+    rowptr, vals = asm["rowptr"], asm["vals"]
+    out = []
+    for c in range(nc):
+        for r in range(5):
+            for k in range(rowptr[c], rowptr[c + 1]):
+                out.append(vals[k, r, :])
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("case", [c for c in G.CASES if c.startswith("implicit")])
+def test_implicit_assembly_matches_reference(case):
+    ref, info = G.load(case)
+    kw = G.oracle_kwargs(info)
+    O = pyoracle.Oracle(G.mesh_of(info), **kw)
+    asm = O.implicit_assemble(kw["cfl"])
+    assert rel_err(asm["rhs"], ref["op_rhs"]) <= TOL
+    assert rel_err(_scalar_csr_vals(asm, O.nc), ref["op_mat_val"]) <= TOL
+
+
+@pytest.mark.parametrize("case", [c for c in G.CASES if c.startswith("implicit")])
+def test_implicit_history_matches_reference(case):
+    ref, info = G.load(case)
+    O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
+    hist = O.implicit_run(info["steps"])
+    refh = ref["implicit_history"].reshape(-1, 12)
+    # RHS L2/max per variable, CFL used, CFL after adaptation
+    assert np.max(np.abs(hist[:, :12] - refh) / np.maximum(np.abs(refh), 1e-300)) <= 1e-10
+    assert rel_err(O.get_state(), ref["final_state"]) <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["kat_subsonic", "kat_supersonic"])
+def test_flux_and_jacobian_kat(name):
+    import numpy as np
+    z = np.load(G.GOLDEN + f"/{name}.npz")
+    inp, out, mach = z["inputs"], z["outputs"], tuple(z["mach"])
+    O = pyoracle.Oracle(G.MESHES["bump_channel_12x4x4_h0.04"](), mach=mach)
+    UL, UR, nh = inp[:, 0:5], inp[:, 5:10], inp[:, 10:13]
+    F, JL, JR = O.flux_batch(0, UL, UR, nh, jacobians=True)
+    assert rel_err(F, out[:, 0:5]) <= TOL
+    assert rel_err(JL.reshape(-1, 25), out[:, 5:30]) <= 1e-12
+    assert rel_err(JR.reshape(-1, 25), out[:, 30:55]) <= 1e-12
+    F, JL, _ = O.flux_batch(1, UL, UR, nh, jacobians=True)
+    assert rel_err(F, out[:, 55:60]) <= TOL
+    assert rel_err(JL.reshape(-1, 25), out[:, 60:85]) <= 1e-12
+    F, JL, _ = O.flux_batch(2, UL, UR, nh, jacobians=True)
+    assert rel_err(F, out[:, 85:90]) <= TOL
+    assert rel_err(JL.reshape(-1, 25), out[:, 90:115]) <= 1e-12
