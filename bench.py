@@ -1,0 +1,316 @@
+"""Benchmark of the steady Euler residual/update path on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+                    [--workload explicit_bump_72k]
+
+A step is one pass of the hot path over the workload: one explicit multi-step iteration
+(4 stages of gradient + limiter + MUSCL, face fluxes and update) over every cell.  The metric
+is cell-updates/s = cells x steps / time.  Rank 0 prints one JSON line.
+
+* value: device time from CUDA events on the library's stream around each step's graph
+  launch, L2 flushed (256 MB write) before every timed step, summed over K steps; max over
+  ranks.
+* e2e: the same steps through the C ABI with host buffers: every step uploads the state,
+  runs one iteration (bes_explicit_iterations, which reads the residual norms back) and
+  downloads the state; wall clock.
+* roofline: the dominant kernel's algorithmic bytes per launch / its average event-timed
+  launch duration, against the measured HBM copy bandwidth.
+* cpu_baseline: the CPU restatement of the reference (OpenMP, all host cores) on a bounded
+  sample of the same workload (rank 0 only).
+N > 1 runs independent replicas (the path has no collective): weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s"
+METRIC_FULL = ("converged solves/hour at 1e-8 residual drop vs plain FP64 GPU; cell-updates/s")
+
+WORKLOADS = {
+    # explicit FP64, 60x20x10-hex bump channel (72,000 tets), Mach 0.5, local dt at CFL 0.8
+    "explicit_bump_72k": dict(kind="explicit", mesh=("bump", 60, 20, 10, 0.04),
+                              opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
+                                        freestream_mach=(0.5, 0.0, 0.0))),
+    # same scheme on the 200x60x30-hex channel (2.16M tets), Mach 0.84
+    "explicit_bump_2m": dict(kind="explicit", mesh=("bump", 200, 60, 30, 0.08),
+                             opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
+                                       freestream_mach=(0.84, 0.0, 0.0))),
+}
+
+# bytes each kernel must move per unit (compulsory traffic of the SoA layout, FP64):
+#   cell sweep per cell: state of the cell (40) + Sc (96) + w (32) + r (96) + adj (16)
+#     + flags (1) + 1/V (8) + eps^2 (8) + face-side state written (40)      = 337
+#     (stage 0 adds plen 24 + V 8 + dt 8 = 40; neighbour states are re-reads of the same array)
+#   face flux per face: RS indices (8) + normal (24) + area (8) + two side states (80)
+#     + flux x area written (40)                                            = 160
+#   update per cell: 4 face ids (16) + 4 fluxes (160) + U(n) (40) + dt (8) + 1/V (8)
+#     + U written (40)                                                      = 272
+BYTES_PER_CELL_SWEEP = 337.0
+BYTES_PER_FACE = 160.0
+BYTES_PER_UPDATE = 272.0
+
+
+def make_mesh(spec):
+    from bes_gb300 import meshgen
+    if spec[0] == "bump":
+        return meshgen.bump_channel(*spec[1:])
+    return meshgen.gaussian_box(*spec[1:])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """Per-launch DRAM bytes of `kernel` from a committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(workload, {}).get(kernel)
+
+
+def cpu_baseline(wl, mesh, steps: int = 2):
+    """The CPU restatement (reference operation order, OpenMP on all host cores)."""
+    from oracle import pyoracle
+    o = wl["opts"]
+    threads = os.cpu_count() or 1
+    O = pyoracle.Oracle(mesh, cfl=o["courant_num"], mach=o["freestream_mach"],
+                        local_dt=o["local_time_step"], threads=threads)
+    O.explicit_run(1)  # warm-up
+    t0 = time.perf_counter()
+    O.explicit_run(steps)
+    dt = time.perf_counter() - t0
+    return {"value": mesh.n_cells * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} explicit iterations on the full {mesh.n_cells}-cell mesh "
+                      f"(oracle/bes_oracle.cpp, OpenMP {threads} threads)"}
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    mesh = make_mesh(wl["mesh"])
+    steps = args.steps
+    from oracle import pyoracle
+    o = wl["opts"]
+    threads = os.cpu_count() or 1
+    O = pyoracle.Oracle(mesh, cfl=o["courant_num"], mach=o["freestream_mach"],
+                        local_dt=o["local_time_step"], threads=threads)
+    O.explicit_run(max(1, min(args.warmup, 2)))
+    # each step: one full explicit iteration on the whole mesh; bounded to about 3 minutes
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(steps):
+        O.explicit_run(1)
+        done += 1
+        if time.perf_counter() - t0 > 180:
+            break
+    dt = time.perf_counter() - t0
+    value = mesh.n_cells * done / dt
+    line = {"impl": "reference", "metric": METRIC, "metric_full": METRIC_FULL, "value": value,
+            "unit": METRIC, "n_gpus": args.gpus, "steps": done, "warmup": args.warmup,
+            "ms_per_step": dt / done * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cells": mesh.n_cells},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": f"{done} explicit iterations on the full mesh; the "
+                                       "reference's CPU path restated in oracle/ (the reference "
+                                       "sources are not available on this host)"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--workload", default="explicit_bump_72k", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local_rank)
+
+    from bes_gb300 import build as nbuild
+    from bes_gb300 import lib
+    nbuild.build()
+    mesh = make_mesh(wl["mesh"])
+    ctx = lib.Context(mesh, lib.default_options(**wl["opts"]))
+    nc, nf = ctx.n_cells, ctx.n_faces
+
+    ctx.enqueue(args.warmup)
+    ctx.synchronize()
+    ext = torch.cuda.ExternalStream(ctx.stream_handle)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kms = np.zeros(4)
+    clocks = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.fill_(float(k))
+            starts[k].record(ext)
+        ctx.enqueue(1)
+        ends[k].record(ext)
+        ext.synchronize()
+        t = ctx.last_kernel_times()
+        kms += np.array([t["cell_ms"], t["face_ms"], t["update_ms"], t["total_ms"]])
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    dev_ms = float(sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
+    t_max = dev_ms
+    if dist:
+        tt = torch.tensor([dev_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * nc * args.steps / (t_max / 1e3)
+
+    # end to end through the C ABI with host buffers
+    U = ctx.get_state()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.set_state(U)
+        ctx.explicit_iterations(1)
+        U = ctx.get_state()
+    e2e_s = time.perf_counter() - t0
+    e2e_max = e2e_s
+    if dist:
+        tt = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_max = float(tt.item())
+    e2e = world * nc * args.steps / e2e_max
+
+    n_stage = 4
+    per_launch = {"cell_recon_kernel": kms[0] / (args.steps * n_stage),
+                  "face_flux_kernel": kms[1] / (args.steps * n_stage),
+                  "update_kernel": kms[2] / (args.steps * n_stage)}
+    bytes_per_launch = {"cell_recon_kernel": BYTES_PER_CELL_SWEEP * nc,
+                        "face_flux_kernel": BYTES_PER_FACE * nf,
+                        "update_kernel": BYTES_PER_UPDATE * nc}
+    dom = max(per_launch, key=lambda k: per_launch[k])
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_per_launch[dom] / (per_launch[dom] / 1e3) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": traffic_from_profiles(dom, args.workload),
+            "ms_per_launch": per_launch[dom], "bytes_per_launch": bytes_per_launch[dom],
+            "kernel_ms_per_step": {"cell_recon_kernel": kms[0] / args.steps,
+                                   "face_flux_kernel": kms[1] / args.steps,
+                                   "update_kernel": kms[2] / args.steps}}
+    line = {"metric": METRIC, "metric_full": METRIC_FULL, "value": value, "unit": METRIC,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cells": nc, "faces": nf,
+                       "parallelism": f"replicas{world}",
+                       "l2": "flushed before every timed step (256 MB write)"},
+            "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": 40 * nc,
+                    "d2h_bytes_per_step": 40 * nc + 80 + 4},
+            "gpu_launches": 14 * args.steps, "roofline": roof, "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl, mesh)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

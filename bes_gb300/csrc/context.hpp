@@ -1,0 +1,81 @@
+// Internal context shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/bes_gb300.h"
+#include "mesh_host.hpp"
+#include "physics.cuh"
+
+namespace bes {
+
+// Device views passed to kernels by value.
+struct DevMesh {
+  int32_t nc, nf, nf_int, nf_slip, nslots, n_extra;
+  const double *vol, *inv_vol, *eps2, *plen;
+  const int32_t *adj, *cface, *gface;
+  const double *Sc, *w, *r;
+  const uint8_t* cflags;
+  const int32_t* extra_cell;
+  const uint8_t* extra_m;
+  const int32_t *fown, *fnb, *fsrc_own, *fsrc_nb;
+  const double *fn, *farea;
+};
+
+struct Params {
+  GasConst gas;
+  double pinf[6];  // freestream primitives (rho, u, v, w, p, T), Config.cpp:480-488
+};
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+};
+
+struct ExplicitGraph {
+  cudaGraphExec_t exec = nullptr;
+};
+
+}  // namespace bes
+
+struct bes_ctx {
+  bes_options opt;
+  bes::RefMesh ref;
+  bes::SoaMesh soa;
+  bes::DevMesh dm;
+  bes::Params prm;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  std::string last_error;
+  std::vector<void*> allocations;  // every device allocation of the context
+  // state: two snapshots (the reference's ping-pong, src/Solution.cpp:63-71)
+  double* U[2] = {nullptr, nullptr};
+  int cur = 0;  // snapshot holding the current state
+  double* RS = nullptr;  // reconstructed face-side states [5][rs_ld]
+  int64_t rs_ld = 0;
+  double* FA = nullptr;  // face flux x area [5][nf]
+  double* dt = nullptr;  // [nc]
+  double* G = nullptr;   // optional gradient output [15][nc]
+  double* PHI = nullptr; // optional limiter output [5][nc]
+  double* Fface = nullptr;  // optional flux per unit area [5][nf]
+  double* R = nullptr;   // optional residual [5][nc]
+  // reductions
+  double* partials = nullptr;  // [10][max_blocks]
+  int max_blocks = 0;
+  unsigned long long* dtmin = nullptr;  // global time step as ordered bits
+  double* hist = nullptr;               // device history [hist_cap][10]
+  int64_t hist_cap = 0;
+  int64_t* iter_ctr = nullptr;
+  int* nan_flag = nullptr;  // face index + 1 of a NaN flux (0 none)
+  // graphs: one explicit iteration for each parity of the current snapshot
+  cudaGraphExec_t it_graph[2] = {nullptr, nullptr};
+  // event pairs around every kernel of an explicit iteration (graph event-record nodes):
+  // [stage][0/1 cell, 2/3 face, 4/5 update]
+  cudaEvent_t kev[8][6] = {};
+  int64_t iterations_done = 0;
+  int64_t iters_since_reset = 0;  // graph launches since the history counter was reset
+};

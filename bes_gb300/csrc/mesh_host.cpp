@@ -1,0 +1,527 @@
+// Host-side mesh pre-processing (runs once per context).
+//
+// Face discovery reproduces Mesh::readGmsh (src/Mesh.cpp:95-558 of joel-ho/BES) with an
+// open-addressing hash table instead of the reference's string-keyed std::map: faces are
+// keyed by their sorted vertex ids, boundary triangles are created first in file order, a
+// tetrahedron's faces follow the local ordering {0,2,1},{1,2,3},{0,3,2},{0,1,3}, the first
+// tetrahedron that meets a face owns it, and boundary normals are flipped to point out of
+// their owner.  Geometry uses the reference's formulas (MeshGmsh.cpp, Element.cpp,
+// MeshCommon.cpp) in the same operation order, including its quirks:
+//   Q1 cell "volume" = sum_f (face centre . S) = 3 x the true volume (MeshGmsh.cpp:101-133);
+//   Q2 cell "centroid" = (v0 + v1 + 2 v2)/4 (MeshGmsh.cpp:135-145);
+//   Q13 MUSCL face vector lookup through a face-id map keyed before ids exist
+//       (Element.cpp:102-105, 185-187): slot 3 for face 0, slot 0 otherwise.
+#include "mesh_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <numeric>
+
+namespace bes {
+
+namespace {
+
+const int kTetFace[4][3] = {{0, 2, 1}, {1, 2, 3}, {0, 3, 2}, {0, 1, 3}};
+
+inline void cross_ref(const double* a, const double* b, const double* c, double* r) {
+  // (c - b) x (a - b)  (MeshMath::crossProduct, src/MeshCommon.cpp:77-96)
+  r[0] = (c[1] - b[1]) * (a[2] - b[2]) - (a[1] - b[1]) * (c[2] - b[2]);
+  r[1] = (a[0] - b[0]) * (c[2] - b[2]) - (c[0] - b[0]) * (a[2] - b[2]);
+  r[2] = (c[0] - b[0]) * (a[1] - b[1]) - (a[0] - b[0]) * (c[1] - b[1]);
+}
+
+// Open-addressing hash map from a sorted vertex triple to a face id.
+class FaceTable {
+ public:
+  explicit FaceTable(size_t expected) {
+    size_t cap = 16;
+    while (cap < expected * 2) cap <<= 1;
+    mask_ = cap - 1;
+    keys_.assign(cap * 3, -1);
+    vals_.assign(cap, -1);
+  }
+  // returns existing id or inserts `id` and returns -1
+  int64_t find_or_insert(const int64_t* k, int64_t id) {
+    size_t h = hash(k) & mask_;
+    while (true) {
+      int64_t* slot = &keys_[h * 3];
+      if (slot[0] < 0) {
+        slot[0] = k[0];
+        slot[1] = k[1];
+        slot[2] = k[2];
+        vals_[h] = id;
+        return -1;
+      }
+      if (slot[0] == k[0] && slot[1] == k[1] && slot[2] == k[2]) return vals_[h];
+      h = (h + 1) & mask_;
+    }
+  }
+  void overwrite(const int64_t* k, int64_t id) {
+    size_t h = hash(k) & mask_;
+    while (true) {
+      int64_t* slot = &keys_[h * 3];
+      if (slot[0] < 0 || (slot[0] == k[0] && slot[1] == k[1] && slot[2] == k[2])) {
+        slot[0] = k[0];
+        slot[1] = k[1];
+        slot[2] = k[2];
+        vals_[h] = id;
+        return;
+      }
+      h = (h + 1) & mask_;
+    }
+  }
+
+ private:
+  static size_t hash(const int64_t* k) {
+    uint64_t h = (uint64_t)k[0] * 0x9E3779B97F4A7C15ull;
+    h ^= (uint64_t)k[1] + 0xC2B2AE3D27D4EB4Full + (h << 6) + (h >> 2);
+    h ^= (uint64_t)k[2] * 0x165667B19E3779F9ull + (h << 6) + (h >> 2);
+    h ^= h >> 29;
+    return (size_t)h;
+  }
+  size_t mask_;
+  std::vector<int64_t> keys_;
+  std::vector<int64_t> vals_;
+};
+
+inline void sort3(int64_t* k) {
+  if (k[0] > k[1]) std::swap(k[0], k[1]);
+  if (k[1] > k[2]) std::swap(k[1], k[2]);
+  if (k[0] > k[1]) std::swap(k[0], k[1]);
+}
+
+}  // namespace
+
+bool build_ref_mesh(const double* X, int64_t nv, const int64_t* btris, const int32_t* btags,
+                    int64_t nb, const int64_t* tets, int64_t nc, bool muscl_exact, RefMesh& M,
+                    std::string& err) {
+  M = RefMesh();
+  if (nc <= 0 || nv <= 0) {
+    err = "empty mesh";
+    return false;
+  }
+  const int64_t nf_est = (4 * nc + nb) / 2 + 16;
+  M.S.reserve(nf_est * 3);
+  M.nhat.reserve(nf_est * 3);
+  M.center.reserve(nf_est * 3);
+  M.area.reserve(nf_est);
+  M.owner.reserve(nf_est);
+  M.neigh.reserve(nf_est);
+  M.kind.reserve(nf_est);
+  FaceTable table((size_t)nf_est);
+  auto new_face = [&](const int64_t* v, int8_t kind) -> int64_t {
+    const int64_t id = (int64_t)M.kind.size();
+    double S[3], c[3];
+    for (int d = 0; d < 3; ++d) c[d] = (X[v[0] * 3 + d] + X[v[1] * 3 + d] + X[v[2] * 3 + d]) / 3;
+    cross_ref(&X[v[0] * 3], &X[v[1] * 3], &X[v[2] * 3], S);
+    double a = 0;
+    for (int d = 0; d < 3; ++d) {
+      S[d] /= 2.0;
+      a += S[d] * S[d];
+    }
+    a = std::sqrt(a);
+    for (int d = 0; d < 3; ++d) {
+      M.S.push_back(S[d]);
+      M.nhat.push_back(S[d] / a);
+      M.center.push_back(c[d]);
+    }
+    M.area.push_back(a);
+    M.owner.push_back(-1);
+    M.neigh.push_back(-1);
+    M.kind.push_back(kind);
+    return id;
+  };
+  for (int64_t b = 0; b < nb; ++b) {
+    const int64_t* v = &btris[b * 3];
+    for (int q = 0; q < 3; ++q)
+      if (v[q] < 0 || v[q] >= nv) {
+        err = "boundary triangle references a missing node";
+        return false;
+      }
+    int8_t kind;
+    if (btags[b] == 1)
+      kind = KIND_SLIP_WALL;
+    else if (btags[b] == 2)
+      kind = KIND_FREESTREAM;
+    else {
+      err = "boundary triangle with an unknown boundary tag " + std::to_string(btags[b]);
+      return false;
+    }
+    int64_t k[3] = {v[0], v[1], v[2]};
+    sort3(k);
+    table.overwrite(k, new_face(v, kind));
+  }
+  M.nc = nc;
+  M.cface.assign(nc * 4, -1);
+  M.cadj.assign(nc * 4, -1);
+  for (int64_t c = 0; c < nc; ++c) {
+    const int64_t* p = &tets[c * 4];
+    for (int q = 0; q < 4; ++q)
+      if (p[q] < 0 || p[q] >= nv) {
+        err = "tetrahedron references a missing node";
+        return false;
+      }
+    for (int m = 0; m < 4; ++m) {
+      const int64_t v[3] = {p[kTetFace[m][0]], p[kTetFace[m][1]], p[kTetFace[m][2]]};
+      int64_t k[3] = {v[0], v[1], v[2]};
+      sort3(k);
+      const int64_t next = (int64_t)M.kind.size();
+      int64_t f = table.find_or_insert(k, next);
+      if (f < 0) {
+        f = new_face(v, KIND_INTERNAL);
+        M.owner[f] = c;
+      } else if (M.kind[f] != KIND_INTERNAL) {
+        double out[3];
+        cross_ref(&X[v[0] * 3], &X[v[1] * 3], &X[v[2] * 3], out);
+        const double dp = M.S[f * 3] * out[0] + M.S[f * 3 + 1] * out[1] + M.S[f * 3 + 2] * out[2];
+        if (dp < 0)
+          for (int d = 0; d < 3; ++d) {
+            M.S[f * 3 + d] = -M.S[f * 3 + d];
+            M.nhat[f * 3 + d] = -M.nhat[f * 3 + d];
+          }
+        M.owner[f] = c;
+        M.neigh[f] = -1;
+      } else {
+        if (M.neigh[f] >= 0) {
+          err = "a face is shared by more than two tetrahedra";
+          return false;
+        }
+        M.neigh[f] = c;
+      }
+      M.cface[c * 4 + m] = f;
+    }
+  }
+  M.nf = (int64_t)M.kind.size();
+  for (int64_t f = 0; f < M.nf; ++f) {
+    if (M.owner[f] < 0) {
+      err = "boundary triangle " + std::to_string(f) + " is not a face of any tetrahedron";
+      return false;
+    }
+    if (M.kind[f] == KIND_INTERNAL && M.neigh[f] < 0) {
+      err = "face " + std::to_string(f) +
+            " belongs to one tetrahedron only and no boundary triangle covers it";
+      return false;
+    }
+  }
+  M.vol.assign(nc, 0);
+  M.centroid.assign(nc * 3, 0);
+  M.rvec.assign(nc * 12, 0);
+  M.weight.assign(nc * 4, 0);
+  M.plen.assign(nc * 3, 0);
+  M.muscl_slot.assign(nc * 4, 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    const int64_t* p = &tets[c * 4];
+    for (int d = 0; d < 3; ++d)
+      M.centroid[c * 3 + d] =
+          (X[p[0] * 3 + d] + X[p[1] * 3 + d] + X[p[2] * 3 + d] + X[p[2] * 3 + d]) / 4;
+    double V = 0;
+    for (int m = 0; m < 4; ++m) {
+      double S[3], C[3];
+      const double* a = &X[p[kTetFace[m][0]] * 3];
+      const double* b = &X[p[kTetFace[m][1]] * 3];
+      const double* e = &X[p[kTetFace[m][2]] * 3];
+      cross_ref(a, b, e, S);
+      double dotp = 0;
+      for (int d = 0; d < 3; ++d) {
+        S[d] /= 2.0;
+        C[d] = ((0.0 + a[d]) + b[d]) + e[d];
+        C[d] /= 3.0;
+      }
+      for (int d = 0; d < 3; ++d) dotp += C[d] * S[d];
+      V += dotp;
+    }
+    M.vol[c] = V;
+    for (int m = 0; m < 4; ++m) {
+      const int64_t f = M.cface[c * 4 + m];
+      for (int d = 0; d < 3; ++d)
+        M.rvec[c * 12 + m * 3 + d] = M.center[f * 3 + d] - M.centroid[c * 3 + d];
+    }
+  }
+  for (int64_t c = 0; c < nc; ++c) {
+    for (int m = 0; m < 4; ++m) {
+      const int64_t f = M.cface[c * 4 + m];
+      if (M.kind[f] == KIND_INTERNAL) M.cadj[c * 4 + m] = (M.owner[f] != c) ? M.owner[f] : M.neigh[f];
+    }
+    for (int m = 0; m < 4; ++m) {
+      const int64_t a = M.cadj[c * 4 + m];
+      if (a < 0) continue;
+      const int64_t f = M.cface[c * 4 + m];
+      double d1 = 0, d2 = 0;
+      for (int d = 0; d < 3; ++d) {
+        const double x1 = M.centroid[c * 3 + d] - M.center[f * 3 + d];
+        const double x2 = M.centroid[a * 3 + d] - M.center[f * 3 + d];
+        d1 += x1 * x1;
+        d2 += x2 * x2;
+      }
+      d1 = std::sqrt(d1);
+      d2 = std::sqrt(d2);
+      M.weight[c * 4 + m] = d2 / (d1 + d2);
+    }
+    for (int m = 0; m < 4; ++m)
+      for (int d = 0; d < 3; ++d) M.plen[c * 3 + d] += std::fabs(M.S[M.cface[c * 4 + m] * 3 + d]);
+    for (int d = 0; d < 3; ++d) M.plen[c * 3 + d] /= 2.0;
+    for (int m = 0; m < 4; ++m)
+      M.muscl_slot[c * 4 + m] = (int8_t)(muscl_exact ? m : (M.cface[c * 4 + m] == 0 ? 3 : 0));
+  }
+  return true;
+}
+
+namespace {
+
+// Reverse Cuthill-McKee on the cell adjacency graph, one BFS per connected component, started
+// from a pseudo-peripheral cell (repeated BFS to the farthest lowest-degree cell).
+std::vector<int64_t> rcm_order(const RefMesh& M) {
+  const int64_t nc = M.nc;
+  std::vector<int> deg(nc, 0);
+  for (int64_t c = 0; c < nc; ++c)
+    for (int m = 0; m < 4; ++m) deg[c] += M.cadj[c * 4 + m] >= 0;
+  std::vector<int64_t> order;
+  order.reserve(nc);
+  std::vector<int64_t> level(nc, -1);
+  std::vector<char> done(nc, 0);
+  std::vector<int64_t> queue;
+  queue.reserve(nc);
+  auto bfs_far = [&](int64_t s) -> int64_t {
+    queue.clear();
+    queue.push_back(s);
+    level[s] = 0;
+    size_t h = 0;
+    int64_t far = s;
+    while (h < queue.size()) {
+      const int64_t c = queue[h++];
+      if (level[c] > level[far] || (level[c] == level[far] && deg[c] < deg[far])) far = c;
+      for (int m = 0; m < 4; ++m) {
+        const int64_t a = M.cadj[c * 4 + m];
+        if (a >= 0 && level[a] < 0) {
+          level[a] = level[c] + 1;
+          queue.push_back(a);
+        }
+      }
+    }
+    for (int64_t c : queue) level[c] = -1;
+    return far;
+  };
+  for (int64_t s0 = 0; s0 < nc; ++s0) {
+    if (done[s0]) continue;
+    int64_t s = bfs_far(s0);
+    s = bfs_far(s);
+    // Cuthill-McKee BFS from s, neighbours by increasing degree
+    const size_t first = order.size();
+    order.push_back(s);
+    done[s] = 1;
+    size_t h = first;
+    while (h < order.size()) {
+      const int64_t c = order[h++];
+      int64_t nb[4];
+      int k = 0;
+      for (int m = 0; m < 4; ++m) {
+        const int64_t a = M.cadj[c * 4 + m];
+        if (a >= 0 && !done[a]) nb[k++] = a;
+      }
+      std::sort(nb, nb + k, [&](int64_t x, int64_t y) {
+        return deg[x] != deg[y] ? deg[x] < deg[y] : x < y;
+      });
+      for (int q = 0; q < k; ++q) {
+        done[nb[q]] = 1;
+        order.push_back(nb[q]);
+      }
+    }
+    std::reverse(order.begin() + first, order.end());
+  }
+  return order;
+}
+
+}  // namespace
+
+void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumber, SoaMesh& S) {
+  S = SoaMesh();
+  const int64_t nc = M.nc, nf = M.nf;
+  S.nc = (int32_t)nc;
+  S.nf = (int32_t)nf;
+  // ---- cells
+  S.cell_new2ref = renumber ? rcm_order(M) : std::vector<int64_t>();
+  if (!renumber) {
+    S.cell_new2ref.resize(nc);
+    std::iota(S.cell_new2ref.begin(), S.cell_new2ref.end(), 0);
+  }
+  S.cell_ref2new.assign(nc, -1);
+  for (int64_t i = 0; i < nc; ++i) S.cell_ref2new[S.cell_new2ref[i]] = i;
+  // ---- faces: interior sorted by (new owner, new neighbour), then slip walls, then
+  // freestream, each group by new owner
+  std::vector<int64_t> fi, fs, ff;
+  for (int64_t f = 0; f < nf; ++f) {
+    if (M.kind[f] == KIND_INTERNAL)
+      fi.push_back(f);
+    else if (M.kind[f] == KIND_SLIP_WALL)
+      fs.push_back(f);
+    else
+      ff.push_back(f);
+  }
+  auto by_owner = [&](int64_t a, int64_t b) {
+    const int64_t oa = S.cell_ref2new[M.owner[a]], ob = S.cell_ref2new[M.owner[b]];
+    if (oa != ob) return oa < ob;
+    const int64_t na = M.neigh[a] >= 0 ? S.cell_ref2new[M.neigh[a]] : -1;
+    const int64_t nb_ = M.neigh[b] >= 0 ? S.cell_ref2new[M.neigh[b]] : -1;
+    if (na != nb_) return na < nb_;
+    return a < b;
+  };
+  std::sort(fi.begin(), fi.end(), by_owner);
+  std::sort(fs.begin(), fs.end(), by_owner);
+  std::sort(ff.begin(), ff.end(), by_owner);
+  S.nf_int = (int32_t)fi.size();
+  S.nf_slip = (int32_t)fs.size();
+  S.nf_free = (int32_t)ff.size();
+  S.face_new2ref.clear();
+  S.face_new2ref.insert(S.face_new2ref.end(), fi.begin(), fi.end());
+  S.face_new2ref.insert(S.face_new2ref.end(), fs.begin(), fs.end());
+  S.face_new2ref.insert(S.face_new2ref.end(), ff.begin(), ff.end());
+  S.face_ref2new.assign(nf, -1);
+  for (int64_t i = 0; i < nf; ++i) S.face_ref2new[S.face_new2ref[i]] = i;
+
+  // ---- reconstructed-state slots
+  S.nslots = muscl_exact ? 4 : 1;
+  // extra (cell, m) pairs whose reference lookup slot is not the cell's main slot 0
+  std::vector<std::pair<int32_t, uint8_t>> extras;
+  if (!muscl_exact)
+    for (int64_t i = 0; i < nc; ++i) {
+      const int64_t c = S.cell_new2ref[i];
+      for (int m = 0; m < 4; ++m) {
+        const int slot = M.muscl_slot[c * 4 + m];
+        if (slot != 0) {
+          bool seen = false;
+          for (auto& e : extras)
+            if (e.first == (int32_t)i && e.second == (uint8_t)slot) seen = true;
+          if (!seen) extras.push_back({(int32_t)i, (uint8_t)slot});
+        }
+      }
+    }
+  std::sort(extras.begin(), extras.end());
+  S.n_extra = (int32_t)extras.size();
+  for (auto& e : extras) {
+    S.extra_cell.push_back(e.first);
+    S.extra_m.push_back(e.second);
+  }
+  auto rs_index = [&](int64_t cnew, int slot) -> int32_t {
+    if (muscl_exact) return (int32_t)(slot * nc + cnew);
+    if (slot == 0) return (int32_t)cnew;
+    for (int32_t k = 0; k < S.n_extra; ++k)
+      if (S.extra_cell[k] == cnew && S.extra_m[k] == slot) return (int32_t)(nc * S.nslots + k);
+    return -1;
+  };
+
+  // ---- cell arrays
+  S.vol.resize(nc);
+  S.inv_vol.resize(nc);
+  S.eps2.resize(nc);
+  S.plen.resize(3 * nc);
+  S.adj.resize(4 * nc);
+  S.cface.resize(4 * nc);
+  S.gface.resize(4 * nc);
+  S.Sc.resize(12 * nc);
+  S.w.resize(4 * nc);
+  S.r.resize(12 * nc);
+  S.cflags.assign(nc, 0);
+  for (int64_t i = 0; i < nc; ++i) {
+    const int64_t c = S.cell_new2ref[i];
+    S.vol[i] = M.vol[c];
+    S.inv_vol[i] = 1.0 / M.vol[c];
+    // epsilon of LimiterVenkatakrishnan (src/LimiterVenkatakrishnan.cpp:42-46), squared
+    const double eps = std::pow(venkat_k * std::pow(M.vol[c], 1.0 / 3), 3.0 / 2.0);
+    S.eps2[i] = eps * eps;
+    for (int d = 0; d < 3; ++d) S.plen[d * nc + i] = M.plen[c * 3 + d];
+    int order[4] = {0, 1, 2, 3};
+    std::sort(order, order + 4,
+              [&](int a, int b) { return M.cface[c * 4 + a] < M.cface[c * 4 + b]; });
+    for (int m = 0; m < 4; ++m) {
+      const int64_t f = M.cface[c * 4 + m];
+      const int64_t a = M.cadj[c * 4 + m];
+      S.adj[m * nc + i] = a >= 0 ? (int32_t)S.cell_ref2new[a] : -1;
+      S.cface[m * nc + i] = (int32_t)S.face_ref2new[f];
+      const double sgn = (M.owner[f] == c) ? 1.0 : -1.0;
+      for (int d = 0; d < 3; ++d) {
+        S.Sc[(m * 3 + d) * nc + i] = sgn * M.S[f * 3 + d];
+        S.r[(m * 3 + d) * nc + i] = M.rvec[c * 12 + m * 3 + d];
+      }
+      S.w[m * nc + i] = M.weight[c * 4 + m];
+      if (M.kind[f] == KIND_SLIP_WALL) S.cflags[i] |= (uint8_t)(1u << m);
+      const int64_t fo = M.cface[c * 4 + order[m]];
+      const int32_t fnew = (int32_t)S.face_ref2new[fo];
+      S.gface[m * nc + i] = (M.owner[fo] == c) ? fnew : ~fnew;
+    }
+  }
+  for (int32_t k = 0; k < S.n_extra; ++k) S.cflags[S.extra_cell[k]] |= 0x10;
+
+  // ---- face arrays
+  S.fown.resize(nf);
+  S.fnb.resize(nf);
+  S.fsrc_own.resize(nf);
+  S.fsrc_nb.resize(nf);
+  S.fn.resize(3 * nf);
+  S.farea.resize(nf);
+  for (int64_t j = 0; j < nf; ++j) {
+    const int64_t f = S.face_new2ref[j];
+    const int64_t o = M.owner[f], n = M.neigh[f];
+    const int64_t on = S.cell_ref2new[o];
+    S.fown[j] = (int32_t)on;
+    S.fnb[j] = n >= 0 ? (int32_t)S.cell_ref2new[n] : -1;
+    int mo = -1, mn = -1;
+    for (int m = 0; m < 4; ++m) {
+      if (M.cface[o * 4 + m] == f) mo = m;
+      if (n >= 0 && M.cface[n * 4 + m] == f) mn = m;
+    }
+    S.fsrc_own[j] = rs_index(on, M.muscl_slot[o * 4 + mo]);
+    S.fsrc_nb[j] = n >= 0 ? rs_index(S.cell_ref2new[n], M.muscl_slot[n * 4 + mn]) : -1;
+    for (int d = 0; d < 3; ++d) S.fn[d * nf + j] = M.nhat[f * 3 + d];
+    S.farea[j] = M.area[f];
+  }
+
+  // ---- implicit block pattern
+  S.brow.assign(nc + 1, 0);
+  for (int64_t i = 0; i < nc; ++i) {
+    int cnt = 1;
+    for (int m = 0; m < 4; ++m) cnt += S.adj[m * nc + i] >= 0;
+    S.brow[i + 1] = S.brow[i] + cnt;
+  }
+  S.bcol.assign(S.brow[nc], 0);
+  S.bdiag.assign(nc, 0);
+  std::vector<int32_t> slot_blk(4 * nc, -1);
+  for (int64_t i = 0; i < nc; ++i) {
+    int32_t k = S.brow[i];
+    S.bdiag[i] = k;
+    S.bcol[k++] = (int32_t)i;
+    for (int m = 0; m < 4; ++m) {
+      const int32_t a = S.adj[m * nc + i];
+      if (a < 0) continue;
+      slot_blk[m * nc + i] = k;
+      S.bcol[k++] = a;
+    }
+  }
+  S.f_blk_on.assign(S.nf_int, -1);
+  S.f_blk_no.assign(S.nf_int, -1);
+  for (int32_t j = 0; j < S.nf_int; ++j) {
+    const int32_t o = S.fown[j], n = S.fnb[j];
+    for (int m = 0; m < 4; ++m) {
+      if (S.cface[m * nc + o] == j) S.f_blk_on[j] = slot_blk[m * nc + o];
+      if (S.cface[m * nc + n] == j) S.f_blk_no[j] = slot_blk[m * nc + n];
+    }
+  }
+  // ---- greedy colouring of the cell graph (no two adjacent cells share a colour)
+  S.cell_color.assign(nc, -1);
+  int32_t ncol = 0;
+  for (int64_t i = 0; i < nc; ++i) {
+    uint32_t used = 0;
+    for (int m = 0; m < 4; ++m) {
+      const int32_t a = S.adj[m * nc + i];
+      if (a >= 0 && S.cell_color[a] >= 0) used |= 1u << S.cell_color[a];
+    }
+    int col = 0;
+    while (used & (1u << col)) ++col;
+    S.cell_color[i] = col;
+    ncol = std::max(ncol, col + 1);
+  }
+  S.n_colors = ncol;
+}
+
+}  // namespace bes

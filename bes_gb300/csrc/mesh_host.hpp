@@ -1,0 +1,57 @@
+// Host-side mesh pre-processing: the reference's face discovery and geometry, its quirks, and
+// the GB300 renumbering into structure-of-arrays.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace bes {
+
+enum FaceKind : int8_t { KIND_INTERNAL = 0, KIND_SLIP_WALL = 1, KIND_FREESTREAM = 2 };
+
+// Mesh with the reference's semantics, in reference numbering (src/Mesh.cpp:95-636).
+struct RefMesh {
+  int64_t nc = 0, nf = 0;
+  std::vector<double> S, nhat, area, center;  // per face [3], [3], [1], [3]
+  std::vector<int64_t> owner, neigh;          // neigh = -1 on boundary faces
+  std::vector<int8_t> kind;
+  std::vector<double> vol, centroid, rvec, weight, plen;  // [1], [3], [4][3], [4], [3] per cell
+  std::vector<int64_t> cface, cadj;                       // [4] per cell
+  std::vector<int8_t> muscl_slot;                         // [4] per cell
+};
+
+// Build from Gmsh-ordered arrays.  Returns false with a message on an unusable mesh.
+bool build_ref_mesh(const double* X, int64_t nv, const int64_t* btris, const int32_t* btags,
+                    int64_t nb, const int64_t* tets, int64_t nc, bool muscl_exact, RefMesh& M,
+                    std::string& err);
+
+// Device-ready arrays after renumbering (all vectors already in the device layout).
+struct SoaMesh {
+  int32_t nc = 0, nf = 0, nf_int = 0, nf_slip = 0, nf_free = 0;
+  int32_t nslots = 1;   // reconstructed states per cell (1 reference lookup, 4 exact)
+  int32_t n_extra = 0;  // extra reconstructed states (reference lookup hitting a slot != 0)
+  std::vector<int64_t> cell_new2ref, cell_ref2new, face_new2ref, face_ref2new;
+  // cells: SoA [k][nc]
+  std::vector<double> vol, inv_vol, eps2, plen;  // plen [3][nc]
+  std::vector<int32_t> adj, cface, gface;        // [4][nc]; gface: faces in reference-id order,
+                                                 // ~f when the cell is the face's neighbour
+  std::vector<double> Sc, w, r;                  // [4*3][nc], [4][nc], [4*3][nc]
+  std::vector<uint8_t> cflags;                   // bit m: face m is a slip wall; bit 4: has extras
+  std::vector<int32_t> extra_cell;               // [n_extra], sorted
+  std::vector<uint8_t> extra_m;                  // [n_extra]
+  // faces: SoA [k][nf]
+  std::vector<int32_t> fown, fnb, fsrc_own, fsrc_nb;  // fnb = -1 on boundary faces
+  std::vector<double> fn, farea;                      // [3][nf], [nf]
+  // block pattern of the implicit matrix (reference CoefficientMatrix, src/CoefficientMatrix.cpp:
+  // 114-164), in new numbering: block row per cell, diagonal first, then neighbours in local
+  // face order.
+  std::vector<int32_t> brow, bcol, bdiag;             // [nc+1], [nblk], [nc]
+  std::vector<int32_t> f_blk_on, f_blk_no;            // per interior face: block (own,nb), (nb,own)
+  std::vector<int32_t> cell_color;                    // greedy colouring of the cell graph
+  int32_t n_colors = 0;
+};
+
+// Reverse Cuthill-McKee renumbering + face grouping + SoA packing.
+void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumber, SoaMesh& out);
+
+}  // namespace bes

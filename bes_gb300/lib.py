@@ -1,0 +1,300 @@
+"""ctypes binding of libbes_gb300.so (include/bes_gb300.h) and a small Python mirror of the
+reference's solver interface (Solver::initialize / setUniversalInitialCondition / solve).
+
+The native library is required: every call goes to the sm_103a CUDA path and fails loudly if
+the library or a GPU is missing.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libbes_gb300.so")
+
+BES_OK = 0
+ERRORS = {1: "BES_ERR_INVALID", 2: "BES_ERR_CUDA", 3: "BES_ERR_NAN", 4: "BES_ERR_MESH",
+          5: "BES_ERR_CONFIG", 6: "BES_ERR_UNSUPPORTED", 7: "BES_ERR_TIMEOUT"}
+
+# every extern "C" symbol declared in include/bes_gb300.h
+EXPORTED = [
+    "bes_options_default", "bes_options_from_besi", "bes_mesh_read_gmsh", "bes_mesh_free",
+    "bes_create", "bes_destroy", "bes_last_error", "bes_sizes", "bes_set_freestream_state",
+    "bes_set_state", "bes_get_state", "bes_compute_operators", "bes_explicit_iterations",
+    "bes_flux_batch", "bes_build_info", "bes_abi_sizes", "bes_host_geometry",
+    "bes_explicit_enqueue", "bes_synchronize", "bes_stream", "bes_last_kernel_times",
+]
+
+
+class BesError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class MeshArrays(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_int64), ("nodes", ctypes.POINTER(ctypes.c_double)),
+                ("n_btris", ctypes.c_int64), ("btris", ctypes.POINTER(ctypes.c_int64)),
+                ("btags", ctypes.POINTER(ctypes.c_int32)), ("n_tets", ctypes.c_int64),
+                ("tets", ctypes.POINTER(ctypes.c_int64))]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [
+        ("solver_type", ctypes.c_int32), ("local_time_step", ctypes.c_int32),
+        ("n_stage", ctypes.c_int32), ("muscl_face_vector", ctypes.c_int32),
+        ("stage_coeff", ctypes.c_double * 8), ("courant_num", ctypes.c_double),
+        ("adaptive_courant_num_max", ctypes.c_double),
+        ("adaptive_courant_num_exponent", ctypes.c_double * 2),
+        ("venkatakrishnan_factor", ctypes.c_double), ("harten_correction_limit", ctypes.c_double),
+        ("gas_constant", ctypes.c_double), ("specific_heat_ratio", ctypes.c_double),
+        ("freestream_mach", ctypes.c_double * 3), ("number_of_time_step", ctypes.c_int32),
+        ("linear_solver", ctypes.c_int32), ("linear_solver_max_iter", ctypes.c_int32),
+        ("gmres_restart", ctypes.c_int32), ("linear_solver_tol", ctypes.c_double),
+        ("jacobian_repeat", ctypes.c_int32), ("precision", ctypes.c_int32),
+        ("cfl_ramp_steps", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("cfl_ramp_start", ctypes.c_double), ("cfl_ramp_end", ctypes.c_double),
+        ("reserved", ctypes.c_double * 4),
+    ]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"native library missing: {path} (run python -m bes_gb300.build)")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    D = ctypes.POINTER(ctypes.c_double)
+    L.bes_options_default.argtypes = [ctypes.POINTER(Options)]
+    L.bes_options_from_besi.argtypes = [ctypes.c_char_p, ctypes.POINTER(Options), ctypes.c_char_p,
+                                        ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t]
+    L.bes_mesh_read_gmsh.argtypes = [ctypes.c_char_p, ctypes.POINTER(MeshArrays),
+                                     ctypes.c_char_p, ctypes.c_size_t]
+    L.bes_mesh_free.argtypes = [ctypes.POINTER(MeshArrays)]
+    L.bes_create.argtypes = [ctypes.POINTER(MeshArrays), ctypes.POINTER(Options),
+                             ctypes.POINTER(P)]
+    L.bes_destroy.argtypes = [P]
+    L.bes_last_error.argtypes = [P]
+    L.bes_last_error.restype = ctypes.c_char_p
+    L.bes_sizes.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.bes_set_freestream_state.argtypes = [P]
+    L.bes_set_state.argtypes = [P, D]
+    L.bes_get_state.argtypes = [P, D]
+    L.bes_compute_operators.argtypes = [P, ctypes.c_double, D, D, D, D, D, D, D]
+    L.bes_explicit_iterations.argtypes = [P, ctypes.c_int64, D]
+    L.bes_flux_batch.argtypes = [P, ctypes.c_int32, ctypes.c_int64, D, D, D, D, D, D]
+    L.bes_build_info.restype = ctypes.c_char_p
+    L.bes_abi_sizes.argtypes = [ctypes.POINTER(ctypes.c_int64)]
+    L.bes_explicit_enqueue.argtypes = [P, ctypes.c_int64]
+    L.bes_synchronize.argtypes = [P]
+    L.bes_stream.argtypes = [P]
+    L.bes_stream.restype = ctypes.c_void_p
+    L.bes_last_kernel_times.argtypes = [P, D]
+    I64 = ctypes.POINTER(ctypes.c_int64)
+    L.bes_host_geometry.argtypes = [ctypes.POINTER(MeshArrays), ctypes.c_int32, I64, I64, D, D, D,
+                                    D, I64, I64, I64, I64, I64, I64, ctypes.c_char_p,
+                                    ctypes.c_size_t]
+    for name in EXTRA_SIGNATURES:
+        fn = getattr(L, name, None)
+        if fn is not None:
+            fn.argtypes, fn.restype = EXTRA_SIGNATURES[name]
+    _lib = L
+    return L
+
+
+EXTRA_SIGNATURES: dict = {}
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    load().bes_options_default(ctypes.byref(o))
+    for k, v in kw.items():
+        if k in ("stage_coeff",):
+            o.n_stage = len(v)
+            for i, x in enumerate(v):
+                o.stage_coeff[i] = float(x)
+        elif k in ("freestream_mach", "adaptive_courant_num_exponent"):
+            arr = getattr(o, k)
+            for i, x in enumerate(v):
+                arr[i] = float(x)
+        else:
+            setattr(o, k, v)
+    return o
+
+
+def options_from_besi(path: str) -> tuple[Options, str]:
+    o = Options()
+    mesh = ctypes.create_string_buffer(4096)
+    err = ctypes.create_string_buffer(512)
+    rc = load().bes_options_from_besi(path.encode(), ctypes.byref(o), mesh, 4096, err, 512)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
+    return o, mesh.value.decode()
+
+
+class _MeshKeep:
+    """Keeps numpy arrays alive for a MeshArrays view."""
+
+    def __init__(self, mesh):
+        self.nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float64)
+        self.tets = np.ascontiguousarray(mesh.tets, dtype=np.int64)
+        self.btris = np.ascontiguousarray(mesh.btris, dtype=np.int64)
+        self.btags = np.ascontiguousarray(mesh.btags, dtype=np.int32)
+        self.c = MeshArrays(self.nodes.shape[0], _d(self.nodes), self.btris.shape[0],
+                            self.btris.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                            self.btags.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                            self.tets.shape[0],
+                            self.tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def host_geometry(mesh, muscl_exact: bool = False) -> dict:
+    """The library's host-side mesh build (no GPU), in reference numbering."""
+    L = load()
+    keep = _MeshKeep(mesh)
+    nc, nf = ctypes.c_int64(), ctypes.c_int64()
+    err = ctypes.create_string_buffer(512)
+    rc = L.bes_host_geometry(ctypes.byref(keep.c), int(muscl_exact), ctypes.byref(nc),
+                             ctypes.byref(nf), None, None, None, None, None, None, None, None,
+                             None, None, err, 512)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
+    nc, nf = nc.value, nf.value
+    g = dict(volume=np.zeros(nc), centroid=np.zeros((nc, 3)), face_S=np.zeros((nf, 3)),
+             face_area=np.zeros(nf), face_owner=np.zeros(nf, np.int64),
+             face_neigh=np.zeros(nf, np.int64), face_type=np.zeros(nf, np.int64),
+             muscl_slot=np.zeros((nc, 4), np.int64), cell_new2ref=np.zeros(nc, np.int64),
+             face_new2ref=np.zeros(nf, np.int64))
+    rc = L.bes_host_geometry(ctypes.byref(keep.c), int(muscl_exact), None, None,
+                             _d(g["volume"]), _d(g["centroid"]), _d(g["face_S"]),
+                             _d(g["face_area"]), _i(g["face_owner"]), _i(g["face_neigh"]),
+                             _i(g["face_type"]), _i(g["muscl_slot"]), _i(g["cell_new2ref"]),
+                             _i(g["face_new2ref"]), err, 512)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
+    return g
+
+
+def read_gmsh(path: str):
+    """Gmsh 2.2 file -> meshgen.TetMesh-like arrays through the library's reader."""
+    from .meshgen import TetMesh
+    L = load()
+    m = MeshArrays()
+    err = ctypes.create_string_buffer(512)
+    rc = L.bes_mesh_read_gmsh(path.encode(), ctypes.byref(m), err, 512)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
+    try:
+        nodes = np.ctypeslib.as_array(m.nodes, shape=(m.n_nodes, 3)).copy()
+        tets = np.ctypeslib.as_array(m.tets, shape=(m.n_tets, 4)).copy()
+        if m.n_btris:
+            btris = np.ctypeslib.as_array(m.btris, shape=(m.n_btris, 3)).copy()
+            btags = np.ctypeslib.as_array(m.btags, shape=(m.n_btris,)).copy().astype(np.int64)
+        else:
+            btris = np.zeros((0, 3), np.int64)
+            btags = np.zeros(0, np.int64)
+    finally:
+        L.bes_mesh_free(ctypes.byref(m))
+    return TetMesh(nodes, tets, btris, btags, name=os.path.basename(path))
+
+
+class Context:
+    """One mesh + options on the current CUDA device (the reference's Solver objects)."""
+
+    def __init__(self, mesh, options: Options):
+        L = load()
+        self._mesh = _MeshKeep(mesh)
+        self.options = options
+        h = ctypes.c_void_p()
+        rc = L.bes_create(ctypes.byref(self._mesh.c), ctypes.byref(options), ctypes.byref(h))
+        if rc != BES_OK:
+            raise BesError(rc, "bes_create failed (mesh or CUDA device)")
+        self.h = h
+        nc, nf = ctypes.c_int64(), ctypes.c_int64()
+        L.bes_sizes(self.h, ctypes.byref(nc), ctypes.byref(nf))
+        self.n_cells, self.n_faces = nc.value, nf.value
+
+    def _check(self, rc):
+        if rc != BES_OK:
+            raise BesError(rc, load().bes_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().bes_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_freestream_state(self):
+        self._check(load().bes_set_freestream_state(self.h))
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(self.n_cells, 5)
+        self._check(load().bes_set_state(self.h, _d(U)))
+
+    def get_state(self) -> np.ndarray:
+        U = np.zeros((self.n_cells, 5))
+        self._check(load().bes_get_state(self.h, _d(U)))
+        return U
+
+    def operators(self, cfl: float) -> dict:
+        nc, nf = self.n_cells, self.n_faces
+        o = dict(dt=np.zeros(nc), grad=np.zeros((nc, 5, 3)), limiter=np.zeros((nc, 5)),
+                 face_UL=np.zeros((nf, 5)), face_UR=np.zeros((nf, 5)), face_flux=np.zeros((nf, 5)),
+                 residual=np.zeros((nc, 5)))
+        self._check(load().bes_compute_operators(
+            self.h, float(cfl), _d(o["dt"]), _d(o["grad"]), _d(o["limiter"]), _d(o["face_UL"]),
+            _d(o["face_UR"]), _d(o["face_flux"]), _d(o["residual"])))
+        return o
+
+    def explicit_iterations(self, n: int, history: bool = True):
+        h = np.zeros((n, 10)) if history else None
+        self._check(load().bes_explicit_iterations(self.h, int(n), _d(h)))
+        return h
+
+    def enqueue(self, n: int):
+        """Enqueue n explicit iterations without waiting."""
+        self._check(load().bes_explicit_enqueue(self.h, int(n)))
+
+    def synchronize(self):
+        self._check(load().bes_synchronize(self.h))
+
+    @property
+    def stream_handle(self) -> int:
+        return int(load().bes_stream(self.h))
+
+    def last_kernel_times(self) -> dict:
+        ms = np.zeros(4)
+        self._check(load().bes_last_kernel_times(self.h, _d(ms)))
+        return dict(cell_ms=ms[0], face_ms=ms[1], update_ms=ms[2], total_ms=ms[3])
+
+    def flux_batch(self, kind: int, UL, UR, nhat, jacobians: bool = False):
+        UL = np.ascontiguousarray(UL, dtype=np.float64)
+        UR = np.ascontiguousarray(UR, dtype=np.float64)
+        nhat = np.ascontiguousarray(nhat, dtype=np.float64)
+        n = UL.shape[0]
+        F = np.zeros((n, 5))
+        JL = np.zeros((n, 5, 5)) if jacobians else None
+        JR = np.zeros((n, 5, 5)) if (jacobians and kind == 0) else None
+        self._check(load().bes_flux_batch(self.h, int(kind), n, _d(UL), _d(UR), _d(nhat), _d(F),
+                                          _d(JL), _d(JR)))
+        return (F, JL, JR) if jacobians else F

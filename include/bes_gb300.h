@@ -1,0 +1,168 @@
+/*
+ * bes_gb300 — GB300-native (sm_103a) steady residual/update path of the Basic Euler Solver
+ * (joel-ho/BES).  Plain C ABI: opaque handle, plain pointers and sizes, int status codes
+ * (0 = ok), no exceptions across the boundary.  All arrays passed in are borrowed and copied;
+ * the library owns its device memory.  One context is used by one host thread at a time and
+ * runs on its own CUDA stream.
+ *
+ * Numbering: every array exchanged through this interface is in the REFERENCE numbering, the
+ * numbering the reference assigns when it reads the same Gmsh file (cells in file order; faces
+ * in creation order: boundary triangles first, then the tetrahedra's new faces).  Internally the
+ * library renumbers cells (reverse Cuthill-McKee) and faces (interior faces sorted by owner,
+ * then slip-wall faces, then freestream faces).
+ *
+ * Layouts: a cell state is [n_cells][5] (rho, rho u, rho v, rho w, rho E); gradients are
+ * [n_cells][5][3]; limiters [n_cells][5]; face fluxes [n_faces][5] per unit area.
+ */
+#ifndef BES_GB300_H
+#define BES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BES_OK 0
+#define BES_ERR_INVALID 1     /* bad argument or size */
+#define BES_ERR_CUDA 2        /* CUDA runtime error or no CUDA device */
+#define BES_ERR_NAN 3         /* NaN in a face flux (the reference exits, src/SolverExplicit.cpp:312-322) */
+#define BES_ERR_MESH 4        /* mesh cannot be used (missing boundary triangle, unknown tag, ...) */
+#define BES_ERR_CONFIG 5      /* .besi option error (unknown key or value, src/Config.cpp:415-418) */
+#define BES_ERR_UNSUPPORTED 6 /* option combination not implemented */
+#define BES_ERR_TIMEOUT 7     /* a bounded device wait gave up */
+
+/* boundary tags of the mesh arrays (the Gmsh physical names SLIP_WALL / FREESTREAM,
+ * src/Options.cpp:22-26) */
+#define BES_TAG_SLIP_WALL 1
+#define BES_TAG_FREESTREAM 2
+
+/* Mesh as read from a Gmsh 2.2 file: nodes, the boundary triangles in file order, then the
+ * tetrahedra in file order.  All ids 0-based. */
+typedef struct {
+  int64_t n_nodes;
+  const double* nodes;   /* [n_nodes][3] */
+  int64_t n_btris;
+  const int64_t* btris;  /* [n_btris][3] */
+  const int32_t* btags;  /* [n_btris] BES_TAG_* */
+  int64_t n_tets;
+  const int64_t* tets;   /* [n_tets][4] positively oriented */
+} bes_mesh_arrays;
+
+/* Options: the .besi keys of the reference (src/Config.cpp:73-422) plus additive keys. */
+typedef struct {
+  int32_t solver_type;            /* SOLVER_TYPE: 0 EXPLICIT, 1 IMPLICIT */
+  int32_t local_time_step;        /* LOCAL_TIME_STEP: 1 YES, 0 NO (default NO) */
+  int32_t n_stage;                /* MULTI_TIME_STEP_OPTIONS: stage count (default 4) */
+  int32_t muscl_face_vector;      /* 0: the reference's lookup (quirk Q13, default); 1: exact */
+  double stage_coeff[8];          /* MULTI_TIME_STEP_OPTIONS coefficients */
+  double courant_num;             /* COURANT_NUM (default 2.0) */
+  double adaptive_courant_num_max;      /* ADAPTIVE_COURANT_NUM_MAX (default 0) */
+  double adaptive_courant_num_exponent[2]; /* ADAPTIVE_COURANT_NUM_EXPONENT (default 1, 1) */
+  double venkatakrishnan_factor;  /* VENKATAKRISHNAN_FACTOR (default 5) */
+  double harten_correction_limit; /* HARTEN_CORRECTION_LIMIT (default 0.05) */
+  double gas_constant;            /* GAS_CONSTANT (default 287) */
+  double specific_heat_ratio;     /* SPECIFIC_HEAT_RATIO (default 1.4) */
+  double freestream_mach[3];      /* FREESTREAM_MACH */
+  int32_t number_of_time_step;    /* NUMBER_OF_TIME_STEP */
+  int32_t linear_solver;          /* 0 block-Jacobi GMRES, 1 block-ILU(0) GMRES */
+  int32_t linear_solver_max_iter; /* LINEAR_SOLVER_MAX_ITER (default 1000) */
+  int32_t gmres_restart;          /* GMRES_RESTART (additive, default 30) */
+  double linear_solver_tol;       /* LINEAR_SOLVER_ABS_TOL: relative to |b| (default 1e-7) */
+  int32_t jacobian_repeat;        /* times each Jacobian block is added (Q9, default 5) */
+  int32_t precision;              /* PRECISION (additive): 0 FP64, 1 FP32 linear solve */
+  int32_t cfl_ramp_steps;         /* CFL_RAMP (additive): steps of a geometric CFL ramp, 0 off */
+  int32_t reserved0;
+  double cfl_ramp_start, cfl_ramp_end;
+  double reserved[4];
+} bes_options;
+
+typedef struct bes_ctx bes_ctx;
+
+/* Default options (Config::setDefaultValues_, src/Config.cpp:73-114). */
+void bes_options_default(bes_options* opt);
+
+/* Parse a .besi file (replaces Config::initialize, src/Config.cpp:116-453): same keys, same
+ * strictness (unknown key -> BES_ERR_CONFIG).  mesh_path receives MESH_FILE. */
+int bes_options_from_besi(const char* besi_path, bes_options* opt, char* mesh_path,
+                          size_t mesh_path_cap, char* err, size_t err_cap);
+
+/* Read a Gmsh 2.2 ASCII mesh (replaces Mesh::readGmsh, src/Mesh.cpp:95-558).  Arrays are
+ * allocated by the library and freed with bes_mesh_free. */
+int bes_mesh_read_gmsh(const char* path, bes_mesh_arrays* out, char* err, size_t err_cap);
+void bes_mesh_free(bes_mesh_arrays* mesh);
+
+/* Create a context on the current CUDA device: build the reference-semantics mesh (face
+ * discovery, geometry, quirks), renumber, upload.  Replaces main()'s Config/Mesh/Gas/Solver
+ * construction (src/BES.cpp:86-106) and Solver::initialize (include/Solver.hpp:70). */
+int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** out);
+void bes_destroy(bes_ctx* ctx);
+const char* bes_last_error(const bes_ctx* ctx);
+int bes_sizes(const bes_ctx* ctx, int64_t* n_cells, int64_t* n_faces);
+
+/* Solver::setUniversalInitialCondition with the freestream primitives (include/Solver.hpp:71). */
+int bes_set_freestream_state(bes_ctx* ctx);
+int bes_set_state(bes_ctx* ctx, const double* U);  /* [n_cells][5] */
+int bes_get_state(bes_ctx* ctx, double* U);        /* [n_cells][5] */
+
+/* Operators at the current state (the reference operator classes):
+ *   TimeStepCalculator::computeAllTimeStep + getTimeStep (TimeStepCalculator.hpp:43-46)
+ *   Gradient::computeGradient + getGradient (Gradient.hpp:46-49)
+ *   Limiter::computeLimiterTerm + getLimiterValue (Limiter.hpp:47-51)
+ *   the face loop's MUSCL states and Flux_<double>::computeFlux (Solver.cpp:69-121,
+ *   Flux.hpp:43-46) and the residual sum R (SolverExplicit.cpp:326-340).
+ * Any output pointer may be NULL. */
+int bes_compute_operators(bes_ctx* ctx, double cfl, double* dt, double* grad, double* limiter,
+                          double* face_UL, double* face_UR, double* face_flux, double* residual);
+
+/* n explicit multi-step iterations (SolverExplicit::timeStep_, src/SolverExplicit.cpp:259-393).
+ * history (may be NULL): [n][10] = L2 and max norm per variable of the last stage's R. */
+int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
+
+/* Per-face fluxes and first-order Jacobians for n independent faces (unit-test entry point;
+ * FluxRoe_/FluxSlipWall_/FluxFreestream_ ::computeFlux and FluxJacobianWrapper_::computeJacobian,
+ * src/FluxJacobianWrapper.tpp:32-82).  kind 0 Roe, 1 slip wall, 2 freestream (UR unused; the
+ * context's freestream).  Host arrays: UL, UR [n][5], nhat [n][3]; F [n][5]; JL, JR [n][5][5]
+ * row-major (JR only for Roe), JL/JR may be NULL. */
+int bes_flux_batch(bes_ctx* ctx, int32_t kind, int64_t n, const double* UL, const double* UR,
+                   const double* nhat, double* F, double* JL, double* JR);
+
+/* Asynchronous form of bes_explicit_iterations for pipelines and benchmarks: enqueue n
+ * iterations (CUDA graph launches) on the context's stream and return without waiting.
+ * bes_synchronize waits and reports a NaN flux or CUDA error of the enqueued work;
+ * bes_stream returns the context's cudaStream_t; bes_last_kernel_times gives the device
+ * milliseconds of the most recent iteration's kernels (ms_out [4]: cell sweep, face flux,
+ * update, sum), read from event pairs captured around every kernel. */
+int bes_explicit_enqueue(bes_ctx* ctx, int64_t n);
+int bes_synchronize(bes_ctx* ctx);
+void* bes_stream(bes_ctx* ctx);
+int bes_last_kernel_times(bes_ctx* ctx, double* ms_out);
+
+/* Library build identification (e.g. "sm_103a"). */
+const char* bes_build_info(void);
+
+/* Sizes of the ABI structs as compiled: out[0] = sizeof(bes_options),
+ * out[1] = sizeof(bes_mesh_arrays).  Lets a binding check its struct mirrors. */
+void bes_abi_sizes(int64_t* out);
+
+/* Host-only (no GPU): the mesh part of bes_create — face discovery, geometry and renumbering —
+ * returned in reference numbering (Mesh::initialize, src/Mesh.cpp:66-93).  Call with NULL
+ * arrays to obtain n_cells / n_faces first.  volume [n_cells], centroid [n_cells][3],
+ * face_S [n_faces][3] (dimensional normal), face_area [n_faces], face_owner / face_neigh
+ * [n_faces] (-1 on boundary), face_kind [n_faces] (0 internal, 1 slip wall, 2 freestream),
+ * muscl_slot [n_cells][4] (local face whose vector the MUSCL reconstruction uses),
+ * cell_new2ref [n_cells] / face_new2ref [n_faces] (the library's internal orders).  Any array
+ * may be NULL. */
+int bes_host_geometry(const bes_mesh_arrays* mesh, int32_t muscl_face_vector, int64_t* n_cells,
+                      int64_t* n_faces, double* volume, double* centroid, double* face_S,
+                      double* face_area, int64_t* face_owner, int64_t* face_neigh,
+                      int64_t* face_kind, int64_t* muscl_slot, int64_t* cell_new2ref,
+                      int64_t* face_new2ref, char* err, size_t err_cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BES_GB300_H */

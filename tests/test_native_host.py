@@ -1,0 +1,161 @@
+"""CPU-only checks of the native library: it loads, exports every symbol the C header
+declares, its struct mirrors match, and its host-side mesh build and .besi / Gmsh readers agree
+with the reference (golden geometry) and with the oracle."""
+import os
+import re
+import tempfile
+
+import numpy as np
+import pytest
+
+from bes_gb300 import build as nbuild
+from bes_gb300 import lib, meshgen
+from tests import _golden as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def native():
+    nbuild.build()
+    return lib.load()
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(bes_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_exports_every_declared_symbol(native):
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(native, n), n
+    assert set(names) == set(lib.EXPORTED)
+
+
+def test_struct_mirrors_match(native):
+    import ctypes
+    out = (ctypes.c_int64 * 2)()
+    native.bes_abi_sizes(out)
+    assert out[0] == ctypes.sizeof(lib.Options)
+    assert out[1] == ctypes.sizeof(lib.MeshArrays)
+
+
+def test_build_info_names_sm103a(native):
+    assert b"sm_103a" in native.bes_build_info()
+
+
+@pytest.mark.parametrize("case", [c for c in G.CASES])
+def test_host_geometry_matches_reference(case):
+    ref, info = G.load(case)
+    if "geo_volume" not in ref:
+        pytest.skip("no geometry dump")
+    g = lib.host_geometry(G.mesh_of(info))
+    for k in ("volume", "centroid", "face_S", "face_area"):
+        np.testing.assert_array_equal(g[k].ravel(), ref["geo_" + k], err_msg=k)
+    for k in ("face_owner", "face_neigh", "face_type", "muscl_slot"):
+        np.testing.assert_array_equal(g[k].ravel(), ref["geo_" + k], err_msg=k)
+
+
+def test_renumbering_is_a_permutation_and_groups_faces():
+    m = meshgen.gaussian_box(10, 6, 10)
+    g = lib.host_geometry(m)
+    nc, nf = m.n_cells, g["face_area"].shape[0]
+    assert np.array_equal(np.sort(g["cell_new2ref"]), np.arange(nc))
+    assert np.array_equal(np.sort(g["face_new2ref"]), np.arange(nf))
+    kinds = g["face_type"][g["face_new2ref"]]
+    # interior faces first, then slip walls, then freestream
+    assert np.all(np.diff(kinds) >= 0)
+
+
+def test_rcm_reduces_bandwidth():
+    m = meshgen.bump_channel(30, 10, 8, 0.04)
+    g = lib.host_geometry(m)
+    inv = np.empty_like(g["cell_new2ref"])
+    inv[g["cell_new2ref"]] = np.arange(len(inv))
+    own, nb = g["face_owner"], g["face_neigh"]
+    mask = nb >= 0
+    bw_new = np.abs(inv[own[mask]] - inv[nb[mask]]).max()
+    bw_old = np.abs(own[mask] - nb[mask]).max()
+    assert bw_new <= bw_old
+
+
+def test_mesh_errors_are_reported():
+    m = meshgen.bump_channel(4, 2, 2, 0.04)
+    bad = meshgen.TetMesh(m.nodes, m.tets, m.btris[2:], m.btags[2:])
+    with pytest.raises(lib.BesError) as e:
+        lib.host_geometry(bad)
+    assert e.value.code == 4
+    bad2 = meshgen.TetMesh(m.nodes, m.tets, m.btris, np.full_like(m.btags, 7))
+    with pytest.raises(lib.BesError):
+        lib.host_geometry(bad2)
+
+
+def test_gmsh_reader_round_trip():
+    m = meshgen.gaussian_box(6, 4, 6)
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "m.msh")
+        meshgen.write_gmsh(m, p)
+        r = lib.read_gmsh(p)
+    np.testing.assert_array_equal(r.nodes, m.nodes)
+    np.testing.assert_array_equal(r.tets, m.tets)
+    np.testing.assert_array_equal(r.btris, m.btris)
+    np.testing.assert_array_equal(r.btags, m.btags)
+
+
+def _write(d, text):
+    p = os.path.join(d, "case.besi")
+    with open(p, "w") as f:
+        f.write(text)
+    return p
+
+
+def test_besi_parser_reference_keys_and_defaults():
+    with tempfile.TemporaryDirectory() as d:
+        p = _write(d, """// comment line
+MESH_FORMAT = GMSH
+MESH_FILE = mesh dir/mesh.msh // trailing comment
+SOLVER_TYPE = IMPLICIT
+LOCAL_TIME_STEP = YES
+COURANT_NUM = 10
+ADAPTIVE_COURANT_NUM_MAX = 1000
+ADAPTIVE_COURANT_NUM_EXPONENT = 0.5, 2
+MULTI_TIME_STEP_OPTIONS = 3, 0.1, 0.5, 1.0
+FREESTREAM_MACH = 0.84, 0.1, 0
+LINEAR_SOLVER = FGMRES
+AMG_PRECOND_COARSENER = SMOOTHED_AGGREGATION
+AMG_PRECOND_SMOOTHER = ILU0
+LINEAR_SOLVER_MAX_ITER = 50
+LINEAR_SOLVER_ABS_TOL = 1e-2
+NUMBER_OF_TIME_STEP = 7
+SAVE_INTERVAL = 10
+""")
+        o, mesh = lib.options_from_besi(p)
+    assert mesh == "meshdir/mesh.msh"  # the reference strips every blank
+    assert o.solver_type == 1 and o.local_time_step == 1
+    assert o.courant_num == 10 and o.adaptive_courant_num_max == 1000
+    assert tuple(o.adaptive_courant_num_exponent) == (0.5, 2.0)
+    assert o.n_stage == 3 and tuple(o.stage_coeff[:3]) == (0.1, 0.5, 1.0)
+    assert tuple(o.freestream_mach) == (0.84, 0.1, 0.0)
+    assert o.linear_solver == 1 and o.linear_solver_max_iter == 50
+    assert o.linear_solver_tol == 1e-2 and o.number_of_time_step == 7
+    # untouched defaults (src/Config.cpp:73-114)
+    assert o.venkatakrishnan_factor == 5.0 and o.harten_correction_limit == 0.05
+    assert o.gas_constant == 287.0 and o.specific_heat_ratio == 1.4
+
+
+@pytest.mark.parametrize("line", ["NOT_A_KEY = 1", "SOLVER_TYPE = SEMI", "FLUX_SCHEME = AUSM",
+                                  "FREESTREAM_MACH = 0.5, 0"])
+def test_besi_parser_is_strict(line):
+    with tempfile.TemporaryDirectory() as d:
+        p = _write(d, "MESH_FORMAT = GMSH\n" + line + "\n")
+        with pytest.raises(lib.BesError) as e:
+            lib.options_from_besi(p)
+    assert e.value.code == 5
