@@ -42,6 +42,10 @@ WORKLOADS = {
     "explicit_bump_72k": dict(kind="explicit", mesh=("bump", 60, 20, 10, 0.04),
                               opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
                                         freestream_mach=(0.5, 0.0, 0.0))),
+    # 120x40x18-hex channel (518,400 tets): a profiling size whose working set exceeds L2
+    "explicit_bump_518k": dict(kind="explicit", mesh=("bump", 120, 40, 18, 0.08),
+                               opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
+                                         freestream_mach=(0.84, 0.0, 0.0))),
     # same scheme on the 200x60x30-hex channel (2.16M tets), Mach 0.84
     "explicit_bump_2m": dict(kind="explicit", mesh=("bump", 200, 60, 30, 0.08),
                              opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,

@@ -82,7 +82,7 @@ void enqueue_iteration(bes_ctx* ctx, int cur) {
   for (int k = 0; k < o.n_stage; ++k) {
     cudaEvent_t* e = ctx->kev[k];
     const double* Uin = (k == 0) ? Un : Uk;
-    cudaEventRecord(e[0], s);
+    cudaEventRecordWithFlags(e[0], s, cudaEventRecordExternal);
     if (k == 0)
       cell_recon_kernel<true, false><<<nb_c, kBlock, 0, s>>>(
           m, ctx->prm, Uin, ctx->RS, ctx->rs_ld, ctx->dt, o.courant_num, local, ctx->dtmin,
@@ -91,19 +91,19 @@ void enqueue_iteration(bes_ctx* ctx, int cur) {
       cell_recon_kernel<false, false><<<nb_c, kBlock, 0, s>>>(
           m, ctx->prm, Uin, ctx->RS, ctx->rs_ld, ctx->dt, o.courant_num, local, ctx->dtmin,
           nullptr, nullptr);
-    cudaEventRecord(e[1], s);
-    cudaEventRecord(e[2], s);
+    cudaEventRecordWithFlags(e[1], s, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(e[2], s, cudaEventRecordExternal);
     face_flux_kernel<false><<<nb_f, kBlock, 0, s>>>(m, ctx->prm, ctx->RS, ctx->rs_ld, ctx->FA,
                                                     nullptr, ctx->nan_flag);
-    cudaEventRecord(e[3], s);
-    cudaEventRecord(e[4], s);
+    cudaEventRecordWithFlags(e[3], s, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(e[4], s, cudaEventRecordExternal);
     if (k == o.n_stage - 1)
       update_kernel<true><<<nb_c, kBlock, 0, s>>>(m, ctx->FA, Un, Uk, ctx->dt, ctx->dtmin, local,
                                                   o.stage_coeff[k], ctx->partials, nullptr);
     else
       update_kernel<false><<<nb_c, kBlock, 0, s>>>(m, ctx->FA, Un, Uk, ctx->dt, ctx->dtmin, local,
                                                    o.stage_coeff[k], ctx->partials, nullptr);
-    cudaEventRecord(e[5], s);
+    cudaEventRecordWithFlags(e[5], s, cudaEventRecordExternal);
   }
   finalize_norms_kernel<<<1, kBlock, 0, s>>>(ctx->partials, nb_c, ctx->hist, ctx->hist_cap,
                                              ctx->iter_ctr);
