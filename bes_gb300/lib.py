@@ -25,6 +25,7 @@ EXPORTED = [
     "bes_set_state", "bes_get_state", "bes_compute_operators", "bes_explicit_iterations",
     "bes_flux_batch", "bes_build_info", "bes_abi_sizes", "bes_host_geometry",
     "bes_explicit_enqueue", "bes_synchronize", "bes_stream", "bes_last_kernel_times",
+    "bes_residual_norms_static",
 ]
 
 
@@ -98,6 +99,8 @@ def load(path: str = LIB_PATH):
     L.bes_stream.argtypes = [P]
     L.bes_stream.restype = ctypes.c_void_p
     L.bes_last_kernel_times.argtypes = [P, D]
+    L.bes_residual_norms_static.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
     I64 = ctypes.POINTER(ctypes.c_int64)
     L.bes_host_geometry.argtypes = [ctypes.POINTER(MeshArrays), ctypes.c_int32, I64, I64, D, D, D,
                                     D, I64, I64, I64, I64, I64, I64, ctypes.c_char_p,
@@ -142,6 +145,16 @@ def options_from_besi(path: str) -> tuple[Options, str]:
     if rc != BES_OK:
         raise BesError(rc, err.value.decode())
     return o, mesh.value.decode()
+
+
+def residual_norms_static(residual_ptr: int, n_cells: int, norms_ptr: int, stream: int = 0):
+    """bes_residual_norms_static on device pointers (no allocation inside the library)."""
+    err = ctypes.create_string_buffer(256)
+    rc = load().bes_residual_norms_static(ctypes.c_void_p(residual_ptr), int(n_cells),
+                                          ctypes.c_void_p(norms_ptr), ctypes.c_void_p(stream),
+                                          err, 256)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
 
 
 class _MeshKeep:

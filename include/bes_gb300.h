@@ -140,6 +140,21 @@ int bes_synchronize(bes_ctx* ctx);
 void* bes_stream(bes_ctx* ctx);
 int bes_last_kernel_times(bes_ctx* ctx, double* ms_out);
 
+/* Residual norms without any device allocation.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc (a framework whose caching allocator already holds
+ * the device memory, or a latency-critical loop where cudaMalloc/cudaFree would synchronise
+ * the device).  Computes, on `stream` (NULL = default stream), the L2 and max norm per variable
+ * of residual [n_cells][5] (device memory, e.g. as laid out by bes_compute_operators) into
+ * norms [10] (device memory: L2[5], then max[5]), with the block reduction of the explicit
+ * iteration.  Its scratch is a fixed 1.25 MiB array in device memory owned by the library
+ * (held on every GPU that loads the library until the process exits), so n_cells is limited to
+ * 4,194,304; larger sizes return BES_ERR_INVALID with a message in err.  The first call on
+ * each device looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  The scratch is shared by all calls:
+ * calls that overlap on the GPU race.  Returns after enqueueing (does not synchronise). */
+int bes_residual_norms_static(const double* residual, int64_t n_cells, double* norms,
+                              void* stream, char* err, size_t err_cap);
+
 /* Library build identification (e.g. "sm_103a"). */
 const char* bes_build_info(void);
 
