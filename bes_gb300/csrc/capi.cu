@@ -134,6 +134,10 @@ void fill_state_aos_to_soa(const bes_ctx* ctx, const double* U, std::vector<doub
 
 }  // namespace
 
+namespace bes {
+int check_nan_public(bes_ctx* ctx) { return check_nan(ctx); }
+}  // namespace bes
+
 extern "C" {
 
 const char* bes_build_info(void) { return "bes_gb300 sm_103a fp64"; }
@@ -241,6 +245,10 @@ int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** ou
   c->prm.pinf[5] = 1.0 / (opt->specific_heat_ratio * opt->gas_constant);
   rc = build_graphs(c);
   if (rc) return rc;
+  if (opt->solver_type == 1) {
+    rc = implicit_allocate(c);
+    if (rc) return rc;
+  }
   rc = bes_set_freestream_state(c);
   if (rc) return rc;
   *out = ctx.release();

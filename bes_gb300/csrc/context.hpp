@@ -42,6 +42,36 @@ struct ExplicitGraph {
 
 }  // namespace bes
 
+namespace bes {
+// Device buffers of the implicit path (allocated when the context is created for it).
+struct ImplicitBuffers {
+  int prec = 0;          // 0: FP64 system, 1: FP32 system (defect correction)
+  size_t tsize = 8;      // sizeof(T)
+  void* A = nullptr;     // ELL blocks [5 slots][25][nc] (factorised in place for ILU)
+  void* Dinv = nullptr;  // [25][nc] inverse diagonal (Jacobi) / inverse U_ii (ILU)
+  void* Dc = nullptr;    // per-face diagonal contributions [2][25][nf]
+  void* b = nullptr;     // right-hand side in T [5][nc]
+  void* V = nullptr;     // Krylov basis [(m+1)][5 nc]
+  void* Z = nullptr;     // [5 nc]
+  void* W = nullptr;     // [5 nc]
+  void* X = nullptr;     // solution dW [5 nc]
+  double* rhs = nullptr;       // FP64 right-hand side [5][nc]
+  double* red = nullptr;       // reduction partials [64][kRedBlocks]
+  double* red_out = nullptr;   // reduced values [64]
+  double* coef = nullptr;      // small coefficient vectors [64]
+  int8_t* m_own = nullptr;     // per face local index in owner / neighbour
+  int8_t* m_nb = nullptr;
+  int32_t* color_rows = nullptr;
+  int32_t* ilu_pos = nullptr;
+  double cfl_actual = 0;
+  double maxres[5] = {0, 0, 0, 0, 0};
+  double maxres_old[5] = {0, 0, 0, 0, 0};
+  int64_t step_count = 0;
+  int last_iters = 0;
+  double last_err = 0;
+};
+}  // namespace bes
+
 struct bes_ctx {
   bes_options opt;
   bes::RefMesh ref;
@@ -78,4 +108,10 @@ struct bes_ctx {
   cudaEvent_t kev[8][6] = {};
   int64_t iterations_done = 0;
   int64_t iters_since_reset = 0;  // graph launches since the history counter was reset
+  bes::ImplicitBuffers imp;
 };
+
+namespace bes {
+int check_nan_public(bes_ctx* ctx);   // synchronises; BES_ERR_NAN if a face flux was NaN
+int implicit_allocate(bes_ctx* ctx);  // buffers of the implicit path
+}  // namespace bes

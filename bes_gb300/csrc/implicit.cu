@@ -1,0 +1,395 @@
+// Implicit (backward-Euler) pseudo-time step on the GPU: SolverImplicit::timeStep_
+// (src/SolverImplicit.cpp:293-345) with the AMGCL solve (src/CoefficientMatrix.cpp:210-325)
+// replaced by right-preconditioned restarted GMRES with a block-Jacobi or colour-ordered
+// block-ILU(0) preconditioner.  The system (Jacobian, preconditioner, Krylov vectors) is FP64
+// for the plain method or FP32 for the defect correction; the residual, right-hand side,
+// update and norms are always FP64.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.hpp"
+#include "implicit_kernels.cuh"
+
+using namespace bes;
+
+namespace {
+
+#define IMP_TRY(ctx, call)                                                       \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess) {                                                     \
+      (ctx)->last_error = std::string(#call) + ": " + cudaGetErrorString(e_);    \
+      return BES_ERR_CUDA;                                                       \
+    }                                                                            \
+  } while (0)
+
+inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+int imp_malloc(bes_ctx* c, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
+  if (e != cudaSuccess) {
+    c->last_error = std::string("cudaMalloc (implicit): ") + cudaGetErrorString(e);
+    return BES_ERR_CUDA;
+  }
+  c->allocations.push_back(*p);
+  return BES_OK;
+}
+
+template <class T>
+struct Sys {
+  bes_ctx* c;
+  int nc;
+  int64_t N;
+  T* A;
+  T* Dinv;
+  T* Dc;
+  T* b;
+  T* V;
+  T* Z;
+  T* W;
+  T* X;
+  cudaStream_t s;
+  explicit Sys(bes_ctx* ctx) : c(ctx) {
+    ImplicitBuffers& I = ctx->imp;
+    nc = ctx->soa.nc;
+    N = 5LL * nc;
+    A = (T*)I.A;
+    Dinv = (T*)I.Dinv;
+    Dc = (T*)I.Dc;
+    b = (T*)I.b;
+    V = (T*)I.V;
+    Z = (T*)I.Z;
+    W = (T*)I.W;
+    X = (T*)I.X;
+    s = ctx->stream;
+  }
+  T* Vk(int k) const { return V + (int64_t)k * N; }
+};
+
+// reduce rows of c->imp.red and copy them to the host
+int reduce_to_host(bes_ctx* c, int nrows, int nblocks, int nsum, int sqrt_sums, double* host) {
+  reduce_rows_kernel<<<nrows, 256, 0, c->stream>>>(c->imp.red, nblocks, nsum, sqrt_sums,
+                                                   c->imp.red_out);
+  IMP_TRY(c, cudaMemcpyAsync(host, c->imp.red_out, nrows * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+  IMP_TRY(c, cudaStreamSynchronize(c->stream));
+  return BES_OK;
+}
+
+template <class T>
+void precond_apply(const Sys<T>& S, const T* in, T* out) {
+  bes_ctx* c = S.c;
+  const SoaMesh& M = c->soa;
+  if (c->opt.linear_solver == 1) {
+    for (int k = 0; k < M.n_colors; ++k) {
+      const int n = M.color_off[k + 1] - M.color_off[k];
+      ilu_lower_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
+                                                         n, c->imp.ilu_pos, S.A, in, out);
+    }
+    for (int k = M.n_colors - 1; k >= 0; --k) {
+      const int n = M.color_off[k + 1] - M.color_off[k];
+      ilu_upper_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
+                                                         n, c->imp.ilu_pos, S.A, S.Dinv, out);
+    }
+  } else {
+    jacobi_apply_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, S.Dinv, in, out);
+  }
+}
+
+template <class T>
+void precond_setup(const Sys<T>& S) {
+  bes_ctx* c = S.c;
+  const SoaMesh& M = c->soa;
+  if (c->opt.linear_solver != 1) return;  // block Jacobi inverted during assembly
+  for (int k = 0; k < M.n_colors; ++k) {
+    const int n = M.color_off[k + 1] - M.color_off[k];
+    ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
+                                                        n, c->imp.ilu_pos, S.A, S.Dinv);
+  }
+}
+
+// Residual, first-order Jacobians and the assembled system at the current state; the FP64
+// right-hand side norms (L2[5], max[5]) are returned in norms10.
+template <class T>
+int assemble(bes_ctx* c, double cfl, double* norms10) {
+  Sys<T> S(c);
+  const DevMesh& m = c->dm;
+  const bes_options& o = c->opt;
+  const int local = o.local_time_step;
+  double* U = c->U[c->cur];
+  reset_dtmin_kernel<<<1, 1, 0, S.s>>>(c->dtmin);
+  cell_recon_kernel<true, false><<<nblk(m.nc, kBlock), kBlock, 0, S.s>>>(
+      m, c->prm, U, c->RS, c->rs_ld, c->dt, cfl, local, c->dtmin, nullptr, nullptr);
+  face_flux_kernel<false><<<nblk(m.nf, kBlock), kBlock, 0, S.s>>>(m, c->prm, c->RS, c->rs_ld,
+                                                                  c->FA, nullptr, c->nan_flag);
+  FaceLocal fl{c->imp.m_own, c->imp.m_nb};
+  face_jacobian_kernel<T><<<nblk(m.nf, 128), 128, 0, S.s>>>(
+      m, c->prm, fl, U, c->dt, c->dtmin, local, o.jacobian_repeat, S.A, S.Dc);
+  const int nb = nblk(m.nc, 128);
+  cell_assemble_kernel<T><<<nb, 128, 0, S.s>>>(m, c->FA, c->dt, c->dtmin, local,
+                                               o.jacobian_repeat, S.Dc, S.A,
+                                               o.linear_solver == 1 ? nullptr : S.Dinv,
+                                               c->imp.rhs, S.b, c->imp.red);
+  IMP_TRY(c, cudaGetLastError());
+  return reduce_to_host(c, 10, nb, 5, 1, norms10);
+}
+
+// Right-preconditioned GMRES(m), x0 = 0, classical Gram-Schmidt with one re-orthogonalisation
+// pass, Givens rotations; stops when |g_{j+1}| <= tol |b| (AMGCL gmres.hpp:163,214 semantics).
+template <class T>
+int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
+  Sys<T> S(c);
+  const bes_options& o = c->opt;
+  const int mr = o.gmres_restart;
+  const int maxiter = o.linear_solver_max_iter;
+  const double tol = o.linear_solver_tol;
+  const int G = kRedBlocks;
+  double* red = c->imp.red;
+  zero_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.N);
+  norm2_kernel<T><<<G, 256, 0, S.s>>>(S.b, S.N, red);
+  double norm_b2;
+  int rc = reduce_to_host(c, 1, G, 1, 0, &norm_b2);
+  if (rc) return rc;
+  const double norm_b = std::sqrt(norm_b2);
+  iters_out = 0;
+  rel_out = 0.0;
+  if (norm_b == 0.0) return BES_OK;
+  const double eps = tol * norm_b;
+  std::vector<double> H((mr + 1) * mr, 0.0), cs(mr), sn(mr), g(mr + 1), h(mr + 1), h2(mr + 1), y(mr);
+  int iter = 0;
+  double norm_r = norm_b;
+  scale_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.b, 1.0, S.N);  // r = b
+  double beta = norm_b;
+  while (true) {
+    if (beta < eps || iter >= maxiter) break;
+    scale_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(0), S.W, 1.0 / beta, S.N);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j = 0;
+    while (j < mr && iter < maxiter) {
+      precond_apply(S, S.Vk(j), S.Z);
+      spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.Z, nullptr, S.W);
+      dots_kernel<T><<<G, 256, 0, S.s>>>(S.V, S.N, j + 1, S.W, S.N, red);
+      if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h.data()))) return rc;
+      IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h.data(), (j + 1) * sizeof(double),
+                                 cudaMemcpyHostToDevice, S.s));
+      axpy_reduce_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j + 1, c->imp.coef, S.N, 1, red);
+      if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h2.data()))) return rc;
+      IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h2.data(), (j + 1) * sizeof(double),
+                                 cudaMemcpyHostToDevice, S.s));
+      axpy_reduce_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j + 1, c->imp.coef, S.N, 2, red);
+      double hn2;
+      if ((rc = reduce_to_host(c, 1, G, 1, 0, &hn2))) return rc;
+      for (int i = 0; i <= j; ++i) H[i * mr + j] = h[i] + h2[i];
+      const double hn = std::sqrt(hn2);
+      H[(j + 1) * mr + j] = hn;
+      if (hn != 0.0) scale_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(j + 1), S.W, 1.0 / hn, S.N);
+      for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * H[i * mr + j] + sn[i] * H[(i + 1) * mr + j];
+        H[(i + 1) * mr + j] = -sn[i] * H[i * mr + j] + cs[i] * H[(i + 1) * mr + j];
+        H[i * mr + j] = t;
+      }
+      const double a = H[j * mr + j], cc = H[(j + 1) * mr + j];
+      const double d = std::sqrt(a * a + cc * cc);
+      cs[j] = (d == 0.0) ? 1.0 : a / d;
+      sn[j] = (d == 0.0) ? 0.0 : cc / d;
+      H[j * mr + j] = d;
+      H[(j + 1) * mr + j] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      ++j;
+      ++iter;
+      if (std::fabs(g[j]) <= eps) break;
+    }
+    for (int i = j - 1; i >= 0; --i) {
+      double s = g[i];
+      for (int k = i + 1; k < j; ++k) s -= H[i * mr + k] * y[k];
+      y[i] = s / H[i * mr + i];
+    }
+    IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, S.s));
+    lincomb_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j, c->imp.coef, S.N);
+    precond_apply(S, S.W, S.Z);
+    add_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.Z, S.N);
+    spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.X, S.b, S.W);  // r = b - A x
+    norm2_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.N, red);
+    double nr2;
+    if ((rc = reduce_to_host(c, 1, G, 1, 0, &nr2))) return rc;
+    norm_r = std::sqrt(nr2);
+    if (norm_r <= eps || iter >= maxiter) break;
+    beta = norm_r;
+  }
+  iters_out = iter;
+  rel_out = norm_r / norm_b;
+  IMP_TRY(c, cudaGetLastError());
+  return BES_OK;
+}
+
+double cfl_for_step(const bes_ctx* c) {
+  const bes_options& o = c->opt;
+  if (o.cfl_ramp_steps > 0) {
+    const int64_t k = c->imp.step_count;
+    if (k >= o.cfl_ramp_steps - 1 || o.cfl_ramp_steps == 1) return o.cfl_ramp_end;
+    const double t = (double)k / (double)(o.cfl_ramp_steps - 1);
+    return o.cfl_ramp_start * std::pow(o.cfl_ramp_end / o.cfl_ramp_start, t);
+  }
+  return c->imp.cfl_actual;
+}
+
+template <class T>
+int implicit_step(bes_ctx* c, double* hist14) {
+  ImplicitBuffers& I = c->imp;
+  const bes_options& o = c->opt;
+  for (int v = 0; v < 5; ++v) I.maxres_old[v] = I.maxres[v];
+  const double cfl = cfl_for_step(c);
+  double norms[10];
+  int rc = assemble<T>(c, cfl, norms);
+  if (rc) return rc;
+  rc = check_nan_public(c);
+  if (rc) return rc;
+  Sys<T> S(c);
+  precond_setup(S);
+  int iters = 0;
+  double rel = 0.0;
+  rc = gmres<T>(c, iters, rel);
+  if (rc) return rc;
+  state_update_kernel<T><<<kRedBlocks, 256, 0, c->stream>>>(c->U[c->cur], S.X, S.N);
+  IMP_TRY(c, cudaGetLastError());
+  for (int v = 0; v < 5; ++v) I.maxres[v] = norms[5 + v];
+  if (o.cfl_ramp_steps <= 0 && o.adaptive_courant_num_max > o.courant_num) {
+    // SolverImplicit::adaptCourantNum_ (src/SolverImplicit.cpp:530-550)
+    const int idx = (I.maxres_old[0] > I.maxres[0]) ? 1 : 0;
+    I.cfl_actual *= std::pow(I.maxres_old[0] / I.maxres[0], o.adaptive_courant_num_exponent[idx]);
+    I.cfl_actual = std::max(o.courant_num, I.cfl_actual);
+    I.cfl_actual = std::min(o.adaptive_courant_num_max, I.cfl_actual);
+  }
+  I.last_iters = iters;
+  I.last_err = rel;
+  if (hist14) {
+    for (int k = 0; k < 10; ++k) hist14[k] = norms[k];
+    hist14[10] = cfl;
+    hist14[11] = I.cfl_actual;
+    hist14[12] = iters;
+    hist14[13] = rel;
+  }
+  ++I.step_count;
+  return BES_OK;
+}
+
+}  // namespace
+
+namespace bes {
+
+int implicit_allocate(bes_ctx* c) {
+  ImplicitBuffers& I = c->imp;
+  const bes_options& o = c->opt;
+  if (o.gmres_restart < 1 || o.gmres_restart > 31) {
+    c->last_error = "GMRES_RESTART must be between 1 and 31";
+    return BES_ERR_UNSUPPORTED;
+  }
+  I.prec = o.precision ? 1 : 0;
+  I.tsize = I.prec ? sizeof(float) : sizeof(double);
+  const SoaMesh& M = c->soa;
+  const int64_t nc = M.nc, nf = M.nf, N = 5 * nc;
+  int rc = 0;
+  rc |= imp_malloc(c, &I.A, 125 * nc * I.tsize);
+  rc |= imp_malloc(c, &I.Dinv, 25 * nc * I.tsize);
+  rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
+  rc |= imp_malloc(c, &I.b, N * I.tsize);
+  rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * N * I.tsize);
+  rc |= imp_malloc(c, &I.Z, N * I.tsize);
+  rc |= imp_malloc(c, &I.W, N * I.tsize);
+  rc |= imp_malloc(c, &I.X, N * I.tsize);
+  rc |= imp_malloc(c, (void**)&I.rhs, N * sizeof(double));
+  rc |= imp_malloc(c, (void**)&I.red, 64 * (size_t)std::max<int64_t>(kRedBlocks, nblk(nc, 128)) * sizeof(double));
+  rc |= imp_malloc(c, (void**)&I.red_out, 64 * sizeof(double));
+  rc |= imp_malloc(c, (void**)&I.coef, 64 * sizeof(double));
+  rc |= imp_malloc(c, (void**)&I.m_own, nf);
+  rc |= imp_malloc(c, (void**)&I.m_nb, nf);
+  rc |= imp_malloc(c, (void**)&I.color_rows, nc * sizeof(int32_t));
+  rc |= imp_malloc(c, (void**)&I.ilu_pos, nc * sizeof(int32_t));
+  if (rc) return BES_ERR_CUDA;
+  IMP_TRY(c, cudaMemset(I.A, 0, 125 * nc * I.tsize));  // empty slots stay zero
+  IMP_TRY(c, cudaMemcpy(I.m_own, M.f_m_own.data(), nf, cudaMemcpyHostToDevice));
+  IMP_TRY(c, cudaMemcpy(I.m_nb, M.f_m_nb.data(), nf, cudaMemcpyHostToDevice));
+  IMP_TRY(c, cudaMemcpy(I.color_rows, M.color_rows.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice));
+  IMP_TRY(c, cudaMemcpy(I.ilu_pos, M.ilu_pos.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice));
+  I.cfl_actual = o.courant_num;
+  return BES_OK;
+}
+
+}  // namespace bes
+
+extern "C" {
+
+int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history) {
+  if (!ctx || n < 0) return BES_ERR_INVALID;
+  if (ctx->opt.solver_type != 1 || !ctx->imp.A) {
+    ctx->last_error = "context was not created for the implicit solver";
+    return BES_ERR_INVALID;
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    int rc = ctx->imp.prec ? implicit_step<float>(ctx, history ? history + i * 14 : nullptr)
+                           : implicit_step<double>(ctx, history ? history + i * 14 : nullptr);
+    if (rc) return rc;
+  }
+  IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BES_OK;
+}
+
+int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks, int64_t* n_blocks) {
+  if (!ctx) return BES_ERR_INVALID;
+  if (ctx->opt.solver_type != 1 || !ctx->imp.A) return BES_ERR_INVALID;
+  const SoaMesh& M = ctx->soa;
+  const RefMesh& R = ctx->ref;
+  const int64_t nc = M.nc;
+  int64_t nb = 0;
+  for (int64_t c = 0; c < nc; ++c) {
+    nb += 1;
+    for (int q = 0; q < 4; ++q) nb += R.cadj[c * 4 + q] >= 0;
+  }
+  if (n_blocks) *n_blocks = nb;
+  if (!rhs && !blocks) return BES_OK;
+  double norms[10];
+  int rc = ctx->imp.prec ? assemble<float>(ctx, cfl, norms) : assemble<double>(ctx, cfl, norms);
+  if (rc) return rc;
+  IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (rhs) {
+    std::vector<double> h(5 * nc);
+    IMP_TRY(ctx, cudaMemcpy(h.data(), ctx->imp.rhs, 5 * nc * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < nc; ++i)
+      for (int v = 0; v < 5; ++v) rhs[M.cell_new2ref[i] * 5 + v] = h[v * nc + i];
+  }
+  if (blocks) {
+    std::vector<double> A(125 * nc);
+    if (ctx->imp.prec) {
+      std::vector<float> Af(125 * nc);
+      IMP_TRY(ctx, cudaMemcpy(Af.data(), ctx->imp.A, Af.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < Af.size(); ++k) A[k] = Af[k];
+    } else {
+      IMP_TRY(ctx, cudaMemcpy(A.data(), ctx->imp.A, A.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    // reference block order: row by reference cell, diagonal first, then neighbours in local
+    // face order (CoefficientMatrix::initialize, src/CoefficientMatrix.cpp:141-160)
+    int64_t k = 0;
+    for (int64_t c = 0; c < nc; ++c) {
+      const int64_t i = M.cell_ref2new[c];
+      for (int s = 0; s < 5; ++s) {
+        if (s > 0 && R.cadj[c * 4 + (s - 1)] < 0) continue;
+        for (int q = 0; q < 25; ++q) blocks[k * 25 + q] = A[(size_t)(s * 25 + q) * nc + i];
+        ++k;
+      }
+    }
+  }
+  return check_nan_public(ctx);
+}
+
+int bes_ilu_order(bes_ctx* ctx, int64_t* order) {
+  if (!ctx || !order) return BES_ERR_INVALID;
+  const SoaMesh& M = ctx->soa;
+  for (int64_t p = 0; p < M.nc; ++p) order[p] = M.cell_new2ref[M.color_rows[p]];
+  return BES_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,565 @@
+// Kernels of the implicit (backward-Euler) path: first-order flux Jacobians, assembly of
+// the 5x5-block system in ELL form, block-Jacobi and colour-ordered block-ILU(0)
+// preconditioners, and the vector kernels of restarted GMRES.  T is the precision of the
+// matrix, preconditioner and Krylov vectors (double for the plain method, float for the
+// defect correction); residuals, right-hand sides and the state stay FP64.
+//
+// ELL layout: value q (= row*5 + col) of slot s of cell i is A[(s*25 + q)*nc + i]; slot 0 is
+// the diagonal block, slot 1+m the block coupling to the neighbour across local face m.
+// Vectors are SoA: component v of cell i is x[v*nc + i].
+#pragma once
+#include "explicit_kernels.cuh"
+
+namespace bes {
+
+constexpr int kRedBlocks = 1024;  // fixed grid of the reduction kernels (deterministic sums)
+
+template <class T>
+__device__ __forceinline__ T& ell(T* A, int s, int q, int nc, int i) {
+  return A[(int64_t)(s * 25 + q) * nc + i];
+}
+template <class T>
+__device__ __forceinline__ T ellc(const T* A, int s, int q, int nc, int i) {
+  return A[(int64_t)(s * 25 + q) * nc + i];
+}
+
+// 5x5 inverse by Gauss-Jordan elimination with partial pivoting.
+template <class T>
+__device__ void inv5(const T* a, T* inv) {
+  T m[5][10];
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      m[i][j] = a[i * 5 + j];
+      m[i][5 + j] = (i == j) ? T(1) : T(0);
+    }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    int p = c;
+#pragma unroll
+    for (int r = c + 1; r < 5; ++r)
+      if (fabs(m[r][c]) > fabs(m[p][c])) p = r;
+    if (p != c)
+#pragma unroll
+      for (int j = 0; j < 10; ++j) {
+        const T t = m[p][j];
+        m[p][j] = m[c][j];
+        m[c][j] = t;
+      }
+    const T piv = T(1) / m[c][c];
+#pragma unroll
+    for (int j = 0; j < 10; ++j) m[c][j] *= piv;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      if (r == c) continue;
+      const T f = m[r][c];
+#pragma unroll
+      for (int j = 0; j < 10; ++j) m[r][j] -= f * m[c][j];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 5; ++i)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) inv[i * 5 + j] = m[i][5 + j];
+}
+
+// ---------------------------------------------------------------------------------------
+// Jacobians and assembly (SolverImplicit::computeFaceFluxes_, src/SolverImplicit.cpp:358-507)
+// ---------------------------------------------------------------------------------------
+struct FaceLocal {
+  const int8_t* m_own;  // local face index of the face in its owner
+  const int8_t* m_nb;   // ... in its neighbour (-1 on boundary faces)
+};
+
+// Per face: dF/dU_L and dF/dU_R at the FIRST-order states (the two cell averages) by
+// forward-mode derivatives of the flux templates (two passes of 5 slots).  Writes the
+// face's two off-diagonal blocks (each added `rep` times from zero, as the reference's
+// addToBlock sits inside the variable loop, quirk Q9) and its contributions to the two
+// diagonal blocks (m_o J_L for the owner, -m_n J_R for the neighbour) for the cell sweep.
+template <class T>
+__global__ void __launch_bounds__(128) face_jacobian_kernel(
+    DevMesh m, Params prm, FaceLocal fl, const double* __restrict__ U,
+    const double* __restrict__ dt, const unsigned long long* __restrict__ dtmin, int local_dt,
+    int rep, T* __restrict__ A, T* __restrict__ Dc) {
+  typedef Dual<5, T> DT;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = m.nc, nf = m.nf;
+  if (f >= nf) return;
+  const int o = m.fown[f];
+  double n[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) n[d] = m.fn[(int64_t)d * nf + f];
+  const double area = m.farea[f];
+  const double dtg = local_dt ? 0.0 : __longlong_as_double((long long)*dtmin);
+  const double m_o = (local_dt ? dt[o] : dtg) * m.inv_vol[o] * area;
+  T JL[25], JR[25];
+  T ul[5], ur[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) ul[v] = (T)U[(int64_t)v * nc + o];
+  const bool interior = f < m.nf_int;
+  int nb = -1;
+  if (interior) {
+    nb = m.fnb[f];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) ur[v] = (T)U[(int64_t)v * nc + nb];
+  }
+  GasConst g = prm.gas;
+  for (int side = 0; side < (interior ? 2 : 1); ++side) {
+    DT dl[5], dr[5], dfl[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      dl[v] = DT(ul[v]);
+      dr[v] = DT(interior ? ur[v] : T(0));
+      if (side == 0)
+        dl[v].d[v] = T(1);
+      else
+        dr[v].d[v] = T(1);
+    }
+    if (interior)
+      roe_flux(g, dl, dr, n, dfl);
+    else if (f < m.nf_int + m.nf_slip)
+      slipwall_flux(g, dl, n, dfl);
+    else
+      freestream_flux(g, dl, prm.pinf, n, dfl);
+    T* J = side == 0 ? JL : JR;
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = 0; b < 5; ++b) J[a * 5 + b] = dfl[a].d[b];
+  }
+  const T mo = (T)m_o;
+#pragma unroll
+  for (int q = 0; q < 25; ++q) Dc[(int64_t)q * nf + f] = mo * JL[q];
+  if (interior) {
+    const double m_n = (local_dt ? dt[nb] : dtg) * m.inv_vol[nb] * area;
+    const T mn = (T)m_n;
+    const int so = 1 + fl.m_own[f], sn = 1 + fl.m_nb[f];
+#pragma unroll
+    for (int q = 0; q < 25; ++q) {
+      Dc[(int64_t)(25 + q) * nf + f] = -mn * JR[q];
+      const T yo = mo * JR[q], yn = -mn * JL[q];
+      T xo = T(0), xn = T(0);
+      for (int r = 0; r < rep; ++r) {
+        xo += yo;
+        xn += yn;
+      }
+      ell(A, so, q, nc, o) = xo;
+      ell(A, sn, q, nc, nb) = xn;
+    }
+  }
+}
+
+// Per cell: right-hand side -(dt/V) sum(+-F A) in the reference's face order, the diagonal
+// block I + rep * sum of the face contributions, block-Jacobi inverse (optional), and block
+// partial norms of the right-hand side.
+template <class T>
+__global__ void __launch_bounds__(128) cell_assemble_kernel(
+    DevMesh m, const double* __restrict__ FA, const double* __restrict__ dt,
+    const unsigned long long* __restrict__ dtmin, int local_dt, int rep, const T* __restrict__ Dc,
+    T* __restrict__ A, T* __restrict__ Dinv, double* __restrict__ rhs, T* __restrict__ rhs_t,
+    double* __restrict__ partials) {
+  const int nc = m.nc, nf = m.nf;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double b[5] = {0, 0, 0, 0, 0};
+  if (i < nc) {
+    const double dti = local_dt ? dt[i] : __longlong_as_double((long long)*dtmin);
+    const double k = dti * m.inv_vol[i];
+    T D[25];
+#pragma unroll
+    for (int q = 0; q < 25; ++q) D[q] = (q % 6 == 0) ? T(1) : T(0);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int gf = m.gface[s * nc + i];
+      const int f = gf >= 0 ? gf : ~gf;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double x = k * FA[(int64_t)v * nf + f];
+        b[v] = gf >= 0 ? b[v] - x : b[v] + x;
+      }
+      const T* src = Dc + (gf >= 0 ? 0 : (int64_t)25 * nf);
+#pragma unroll
+      for (int q = 0; q < 25; ++q) {
+        const T y = src[(int64_t)q * nf + f];
+        for (int r = 0; r < rep; ++r) D[q] += y;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 25; ++q) ell(A, 0, q, nc, i) = D[q];
+    if (Dinv) {
+      T inv[25];
+      inv5(D, inv);
+#pragma unroll
+      for (int q = 0; q < 25; ++q) Dinv[(int64_t)q * nc + i] = inv[q];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      rhs[(int64_t)v * nc + i] = b[v];
+      rhs_t[(int64_t)v * nc + i] = (T)b[v];
+    }
+  }
+  __shared__ double sh[10][4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const double s2 = warp_sum(b[v] * b[v]);
+    const double mx = warp_max(fabs(b[v]));
+    if (lane == 0) {
+      sh[v][wid] = s2;
+      sh[5 + v][wid] = mx;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int q = 0; q < 10; ++q) {
+      double x = lane < 4 ? sh[q][lane] : 0.0;
+      x = q < 5 ? warp_sum(x) : warp_max(x);
+      if (lane == 0) partials[(int64_t)q * gridDim.x + blockIdx.x] = x;
+    }
+  }
+}
+
+// Reduce `nvals` rows of per-block partials (sums, or maxima for rows >= nsum) in a fixed
+// order; one block per value.  out[k] = sum (sqrt if sqrt_sums) or max.
+__global__ void __launch_bounds__(256) reduce_rows_kernel(const double* __restrict__ partials,
+                                                          int nblocks, int nsum, int sqrt_sums,
+                                                          double* __restrict__ out) {
+  __shared__ double sh[8];
+  const int k = blockIdx.x;
+  const bool is_sum = k < nsum;
+  double x = is_sum ? 0.0 : 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    const double y = partials[(int64_t)k * nblocks + b];
+    x = is_sum ? x + y : fmax(x, y);
+  }
+  x = is_sum ? warp_sum(x) : warp_max(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = x;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    x = lane < 8 ? sh[lane] : 0.0;
+    x = is_sum ? warp_sum(x) : warp_max(x);
+    if (lane == 0) out[k] = (is_sum && sqrt_sums) ? sqrt(x) : x;
+  }
+}
+
+// Colour-ordered block ILU(0), one colour per launch (rows of one colour are independent).
+// IKJ order: the lower blocks of a row are eliminated in increasing factorisation position.
+template <class T>
+__global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_t* __restrict__ rows,
+                                                         int nrows, const int32_t* __restrict__ pos,
+                                                         T* __restrict__ A, T* __restrict__ Dinv) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows) return;
+  const int nc = m.nc;
+  const int i = rows[t];
+  const int pi = pos[i];
+  int nbr[4], pn[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    nbr[s] = m.adj[s * nc + i];
+    pn[s] = nbr[s] >= 0 ? pos[nbr[s]] : 0x7fffffff;
+  }
+  // lower slots sorted by position
+  int lo[4], nl = 0;
+  for (int s = 0; s < 4; ++s)
+    if (nbr[s] >= 0 && pn[s] < pi) lo[nl++] = s;
+  for (int a = 1; a < nl; ++a)
+    for (int b = a; b > 0 && pn[lo[b]] < pn[lo[b - 1]]; --b) {
+      const int x = lo[b];
+      lo[b] = lo[b - 1];
+      lo[b - 1] = x;
+    }
+  for (int li = 0; li < nl; ++li) {
+    const int s = lo[li];
+    const int j = nbr[s];
+    const int pj = pn[s];
+    T L[25];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) acc += ell(A, 1 + s, r * 5 + k, nc, i) * Dinv[(int64_t)(k * 5 + c) * nc + j];
+        L[r * 5 + c] = acc;
+      }
+#pragma unroll
+    for (int q = 0; q < 25; ++q) ell(A, 1 + s, q, nc, i) = L[q];
+    // A_ik -= L_ij U_jk for every k in row i's pattern with pos(k) > pos(j) and (j,k) present
+    for (int kk = -1; kk < 4; ++kk) {
+      const int col = kk < 0 ? i : nbr[kk];
+      if (kk >= 0 && (col < 0 || pn[kk] <= pj)) continue;
+      int sj = -1;
+      for (int q = 0; q < 4; ++q)
+        if (m.adj[q * nc + j] == col) sj = q;
+      if (sj < 0) continue;
+      const int dst = kk < 0 ? 0 : 1 + kk;
+#pragma unroll
+      for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          T acc = T(0);
+#pragma unroll
+          for (int k = 0; k < 5; ++k) acc += L[r * 5 + k] * ell(A, 1 + sj, k * 5 + c, nc, j);
+          ell(A, dst, r * 5 + c, nc, i) -= acc;
+        }
+    }
+  }
+  T D[25], inv[25];
+#pragma unroll
+  for (int q = 0; q < 25; ++q) D[q] = ell(A, 0, q, nc, i);
+  inv5(D, inv);
+#pragma unroll
+  for (int q = 0; q < 25; ++q) Dinv[(int64_t)q * nc + i] = inv[q];
+}
+
+// forward solve of one colour: out_i = in_i - sum_{lower j} L_ij out_j
+template <class T>
+__global__ void __launch_bounds__(128) ilu_lower_kernel(DevMesh m, const int32_t* __restrict__ rows,
+                                                        int nrows, const int32_t* __restrict__ pos,
+                                                        const T* __restrict__ A,
+                                                        const T* __restrict__ in, T* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows) return;
+  const int nc = m.nc;
+  const int i = rows[t];
+  const int pi = pos[i];
+  T acc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = in[(int64_t)v * nc + i];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int j = m.adj[s * nc + i];
+    if (j < 0 || pos[j] >= pi) continue;
+    T y[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) y[v] = out[(int64_t)v * nc + j];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[r] -= ellc(A, 1 + s, r * 5 + c, nc, i) * y[c];
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) out[(int64_t)v * nc + i] = acc[v];
+}
+
+// backward solve of one colour, in place: z_i = inv(U_ii) (y_i - sum_{upper k} U_ik z_k)
+template <class T>
+__global__ void __launch_bounds__(128) ilu_upper_kernel(DevMesh m, const int32_t* __restrict__ rows,
+                                                        int nrows, const int32_t* __restrict__ pos,
+                                                        const T* __restrict__ A,
+                                                        const T* __restrict__ Dinv, T* __restrict__ z) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows) return;
+  const int nc = m.nc;
+  const int i = rows[t];
+  const int pi = pos[i];
+  T acc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = z[(int64_t)v * nc + i];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int k = m.adj[s * nc + i];
+    if (k < 0 || pos[k] <= pi) continue;
+    T y[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) y[v] = z[(int64_t)v * nc + k];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[r] -= ellc(A, 1 + s, r * 5 + c, nc, i) * y[c];
+  }
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    T x = T(0);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) x += Dinv[(int64_t)(r * 5 + c) * nc + i] * acc[c];
+    z[(int64_t)r * nc + i] = x;
+  }
+}
+
+// block-Jacobi application: out_i = Dinv_i in_i
+template <class T>
+__global__ void __launch_bounds__(256) jacobi_apply_kernel(int nc, const T* __restrict__ Dinv,
+                                                           const T* __restrict__ in,
+                                                           T* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  T x[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) x[v] = in[(int64_t)v * nc + i];
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    T acc = T(0);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) acc += Dinv[(int64_t)(r * 5 + c) * nc + i] * x[c];
+    out[(int64_t)r * nc + i] = acc;
+  }
+}
+
+// y = A x (ELL), optionally y = b - A x
+template <class T>
+__global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restrict__ A,
+                                                   const T* __restrict__ x,
+                                                   const T* __restrict__ b, T* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = m.nc;
+  if (i >= nc) return;
+  T acc[5], xi[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)v * nc + i];
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    T s = T(0);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) s += ellc(A, 0, r * 5 + c, nc, i) * xi[c];
+    acc[r] = s;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = m.adj[q * nc + i];
+    if (j < 0) continue;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)v * nc + j];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[r] += ellc(A, 1 + q, r * 5 + c, nc, i) * xi[c];
+  }
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+    y[(int64_t)r * nc + i] = b ? b[(int64_t)r * nc + i] - acc[r] : acc[r];
+}
+
+// partial dots: partials[k*G + blk] = sum V_k . w over the block's grid-stride range
+template <class T>
+__global__ void __launch_bounds__(256) dots_kernel(const T* __restrict__ V, int64_t ldv, int nvec,
+                                                   const T* __restrict__ w, int64_t N,
+                                                   double* __restrict__ partials) {
+  __shared__ double sh[8];
+  for (int k = 0; k < nvec; ++k) {
+    const T* vk = V + (int64_t)k * ldv;
+    double s = 0.0;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+         idx += (int64_t)gridDim.x * blockDim.x)
+      s += (double)vk[idx] * (double)w[idx];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double x = threadIdx.x < 8 ? sh[threadIdx.x] : 0.0;
+      x = warp_sum(x);
+      if (threadIdx.x == 0) partials[(int64_t)k * gridDim.x + blockIdx.x] = x;
+    }
+    __syncthreads();
+  }
+}
+
+// w -= sum_k h_k V_k; then (mode 1) partial dots V_k . w_new, or (mode 2) partial |w_new|^2
+template <class T>
+__global__ void __launch_bounds__(256) axpy_reduce_kernel(T* __restrict__ w, const T* __restrict__ V,
+                                                          int64_t ldv, int nvec,
+                                                          const double* __restrict__ h, int64_t N,
+                                                          int mode, double* __restrict__ partials) {
+  __shared__ double sh[32][8];
+  __shared__ double hs[64];
+  for (int k = threadIdx.x; k < nvec; k += blockDim.x) hs[k] = h[k];
+  __syncthreads();
+  double acc[32];
+  const int nacc = mode == 1 ? nvec : 1;
+  for (int k = 0; k < nacc; ++k) acc[k] = 0.0;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    double x = (double)w[idx];
+    for (int k = 0; k < nvec; ++k) x -= hs[k] * (double)V[(int64_t)k * ldv + idx];
+    const T xt = (T)x;
+    w[idx] = xt;
+    if (mode == 1) {
+      for (int k = 0; k < nvec; ++k) acc[k] += (double)V[(int64_t)k * ldv + idx] * (double)xt;
+    } else {
+      acc[0] += (double)xt * (double)xt;
+    }
+  }
+  for (int k = 0; k < nacc; ++k) {
+    const double s = warp_sum(acc[k]);
+    if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nacc; k += blockDim.x) {
+    double s = 0.0;
+    for (int q = 0; q < 8; ++q) s += sh[k][q];
+    partials[(int64_t)k * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) scale_kernel(T* __restrict__ out, const T* __restrict__ in,
+                                                    double s, int64_t N) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    out[idx] = (T)((double)in[idx] * s);
+}
+
+// out = sum_k y_k V_k
+template <class T>
+__global__ void __launch_bounds__(256) lincomb_kernel(T* __restrict__ out, const T* __restrict__ V,
+                                                      int64_t ldv, int nvec,
+                                                      const double* __restrict__ y, int64_t N) {
+  __shared__ double ys[64];
+  for (int k = threadIdx.x; k < nvec; k += blockDim.x) ys[k] = y[k];
+  __syncthreads();
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    double x = 0.0;
+    for (int k = 0; k < nvec; ++k) x += ys[k] * (double)V[(int64_t)k * ldv + idx];
+    out[idx] = (T)x;
+  }
+}
+
+// x += z
+template <class T>
+__global__ void __launch_bounds__(256) add_kernel(T* __restrict__ x, const T* __restrict__ z,
+                                                  int64_t N) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    x[idx] += z[idx];
+}
+
+// partial |x|^2
+template <class T>
+__global__ void __launch_bounds__(256) norm2_kernel(const T* __restrict__ x, int64_t N,
+                                                    double* __restrict__ partials) {
+  __shared__ double sh[8];
+  double s = 0.0;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    s += (double)x[idx] * (double)x[idx];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < 8 ? sh[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+  }
+}
+
+// state update W += dW (SolverImplicit::updateSolution_, src/SolverImplicit.cpp:509-528)
+template <class T>
+__global__ void __launch_bounds__(256) state_update_kernel(double* __restrict__ U,
+                                                           const T* __restrict__ dW, int64_t N) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    U[idx] += (double)dW[idx];
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) zero_kernel(T* __restrict__ x, int64_t N) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    x[idx] = T(0);
+}
+
+}  // namespace bes

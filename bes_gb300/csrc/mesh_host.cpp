@@ -477,34 +477,14 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
     S.farea[j] = M.area[f];
   }
 
-  // ---- implicit block pattern
-  S.brow.assign(nc + 1, 0);
-  for (int64_t i = 0; i < nc; ++i) {
-    int cnt = 1;
-    for (int m = 0; m < 4; ++m) cnt += S.adj[m * nc + i] >= 0;
-    S.brow[i + 1] = S.brow[i] + cnt;
-  }
-  S.bcol.assign(S.brow[nc], 0);
-  S.bdiag.assign(nc, 0);
-  std::vector<int32_t> slot_blk(4 * nc, -1);
-  for (int64_t i = 0; i < nc; ++i) {
-    int32_t k = S.brow[i];
-    S.bdiag[i] = k;
-    S.bcol[k++] = (int32_t)i;
-    for (int m = 0; m < 4; ++m) {
-      const int32_t a = S.adj[m * nc + i];
-      if (a < 0) continue;
-      slot_blk[m * nc + i] = k;
-      S.bcol[k++] = a;
-    }
-  }
-  S.f_blk_on.assign(S.nf_int, -1);
-  S.f_blk_no.assign(S.nf_int, -1);
-  for (int32_t j = 0; j < S.nf_int; ++j) {
+  // ---- ELL slots of each face in its two cells
+  S.f_m_own.assign(nf, -1);
+  S.f_m_nb.assign(nf, -1);
+  for (int64_t j = 0; j < nf; ++j) {
     const int32_t o = S.fown[j], n = S.fnb[j];
     for (int m = 0; m < 4; ++m) {
-      if (S.cface[m * nc + o] == j) S.f_blk_on[j] = slot_blk[m * nc + o];
-      if (S.cface[m * nc + n] == j) S.f_blk_no[j] = slot_blk[m * nc + n];
+      if (S.cface[m * nc + o] == j) S.f_m_own[j] = (int8_t)m;
+      if (n >= 0 && S.cface[m * nc + n] == j) S.f_m_nb[j] = (int8_t)m;
     }
   }
   // ---- greedy colouring of the cell graph (no two adjacent cells share a colour)
@@ -522,6 +502,19 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
     ncol = std::max(ncol, col + 1);
   }
   S.n_colors = ncol;
+  S.color_off.assign(ncol + 1, 0);
+  for (int64_t i = 0; i < nc; ++i) S.color_off[S.cell_color[i] + 1]++;
+  for (int c = 0; c < ncol; ++c) S.color_off[c + 1] += S.color_off[c];
+  S.color_rows.assign(nc, 0);
+  S.ilu_pos.assign(nc, 0);
+  {
+    std::vector<int32_t> fill(S.color_off.begin(), S.color_off.end() - 1);
+    for (int64_t i = 0; i < nc; ++i) {
+      const int32_t p = fill[S.cell_color[i]]++;
+      S.color_rows[p] = (int32_t)i;
+      S.ilu_pos[i] = p;
+    }
+  }
 }
 
 }  // namespace bes

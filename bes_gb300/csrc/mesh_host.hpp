@@ -42,12 +42,15 @@ struct SoaMesh {
   // faces: SoA [k][nf]
   std::vector<int32_t> fown, fnb, fsrc_own, fsrc_nb;  // fnb = -1 on boundary faces
   std::vector<double> fn, farea;                      // [3][nf], [nf]
-  // block pattern of the implicit matrix (reference CoefficientMatrix, src/CoefficientMatrix.cpp:
-  // 114-164), in new numbering: block row per cell, diagonal first, then neighbours in local
-  // face order.
-  std::vector<int32_t> brow, bcol, bdiag;             // [nc+1], [nblk], [nc]
-  std::vector<int32_t> f_blk_on, f_blk_no;            // per interior face: block (own,nb), (nb,own)
-  std::vector<int32_t> cell_color;                    // greedy colouring of the cell graph
+  // implicit matrix in ELL form: per cell, slot 0 = diagonal block, slot 1+m = the block of
+  // the neighbour across local face m (empty for boundary faces).  This is the reference's
+  // block pattern (CoefficientMatrix::initialize, src/CoefficientMatrix.cpp:114-164: the
+  // diagonal block first, then neighbours in local face order) with fixed-width rows.
+  std::vector<int8_t> f_m_own, f_m_nb;   // local face index of each face in owner / neighbour
+  std::vector<int32_t> cell_color;       // greedy colouring of the cell graph
+  std::vector<int32_t> color_rows;       // cells sorted by (colour, id): the ILU(0) order
+  std::vector<int32_t> color_off;        // [n_colors+1] offsets into color_rows
+  std::vector<int32_t> ilu_pos;          // cell -> position in color_rows
   int32_t n_colors = 0;
 };
 

@@ -25,7 +25,8 @@ EXPORTED = [
     "bes_set_state", "bes_get_state", "bes_compute_operators", "bes_explicit_iterations",
     "bes_flux_batch", "bes_build_info", "bes_abi_sizes", "bes_host_geometry",
     "bes_explicit_enqueue", "bes_synchronize", "bes_stream", "bes_last_kernel_times",
-    "bes_residual_norms_static",
+    "bes_residual_norms_static", "bes_implicit_steps", "bes_implicit_assemble",
+    "bes_ilu_order",
 ]
 
 
@@ -99,6 +100,9 @@ def load(path: str = LIB_PATH):
     L.bes_stream.argtypes = [P]
     L.bes_stream.restype = ctypes.c_void_p
     L.bes_last_kernel_times.argtypes = [P, D]
+    L.bes_implicit_steps.argtypes = [P, ctypes.c_int64, D]
+    L.bes_implicit_assemble.argtypes = [P, ctypes.c_double, D, D, ctypes.POINTER(ctypes.c_int64)]
+    L.bes_ilu_order.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_residual_norms_static.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
     I64 = ctypes.POINTER(ctypes.c_int64)
@@ -299,6 +303,26 @@ class Context:
         ms = np.zeros(4)
         self._check(load().bes_last_kernel_times(self.h, _d(ms)))
         return dict(cell_ms=ms[0], face_ms=ms[1], update_ms=ms[2], total_ms=ms[3])
+
+    def implicit_steps(self, n: int):
+        """n implicit steps; history [n, 14] (see bes_implicit_steps)."""
+        h = np.zeros((n, 14))
+        self._check(load().bes_implicit_steps(self.h, int(n), _d(h)))
+        return h
+
+    def implicit_assemble(self, cfl: float) -> dict:
+        nb = ctypes.c_int64()
+        self._check(load().bes_implicit_assemble(self.h, float(cfl), None, None, ctypes.byref(nb)))
+        rhs = np.zeros((self.n_cells, 5))
+        blocks = np.zeros((nb.value, 5, 5))
+        self._check(load().bes_implicit_assemble(self.h, float(cfl), _d(rhs), _d(blocks),
+                                                 ctypes.byref(nb)))
+        return dict(rhs=rhs, blocks=blocks)
+
+    def ilu_order(self) -> np.ndarray:
+        o = np.zeros(self.n_cells, np.int64)
+        self._check(load().bes_ilu_order(self.h, _i(o)))
+        return o
 
     def flux_batch(self, kind: int, UL, UR, nhat, jacobians: bool = False):
         UL = np.ascontiguousarray(UL, dtype=np.float64)

@@ -121,6 +121,28 @@ int bes_compute_operators(bes_ctx* ctx, double cfl, double* dt, double* grad, do
  * history (may be NULL): [n][10] = L2 and max norm per variable of the last stage's R. */
 int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
 
+/* n implicit pseudo-time steps (SolverImplicit::timeStep_, src/SolverImplicit.cpp:293-345):
+ * local/global dt at the step's CFL, second-order residual, first-order Jacobians assembled
+ * into the 5x5-block system (each block added jacobian_repeat times, Q9), right-preconditioned
+ * GMRES(gmres_restart) to linear_solver_tol relative with a block-Jacobi (linear_solver 0) or
+ * colour-ordered block-ILU(0) (linear_solver 1) preconditioner, in FP64 (precision 0) or FP32
+ * (precision 1, defect correction: residual, update and norms stay FP64), the update, and the
+ * CFL control (adaptive as adaptCourantNum_, src/SolverImplicit.cpp:530-550, or the additive
+ * geometric ramp).  history (may be NULL): [n][14] = L2[5] and max[5] of the Dt/V-scaled
+ * right-hand side (the max is what the reference logs, Q10), CFL used, CFL after the step,
+ * linear iterations, final relative linear residual. */
+int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history);
+
+/* Assemble (without solving or updating) the implicit system at the current state and CFL
+ * (SolverImplicit::computeFaceFluxes_ and the CoefficientMatrix, src/SolverImplicit.cpp:358-507).
+ * rhs [n_cells][5]; blocks [n_blocks][5][5] row-major in the reference's block order (row by
+ * cell, diagonal block first, then neighbours in local face order,
+ * src/CoefficientMatrix.cpp:141-160).  Pass NULL arrays to query n_blocks. */
+int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks, int64_t* n_blocks);
+
+/* The block-ILU(0) factorisation order (reference cell ids, colour by colour). */
+int bes_ilu_order(bes_ctx* ctx, int64_t* order);
+
 /* Per-face fluxes and first-order Jacobians for n independent faces (unit-test entry point;
  * FluxRoe_/FluxSlipWall_/FluxFreestream_ ::computeFlux and FluxJacobianWrapper_::computeJacobian,
  * src/FluxJacobianWrapper.tpp:32-82).  kind 0 Roe, 1 slip wall, 2 freestream (UR unused; the

@@ -1,0 +1,111 @@
+"""GPU parity of the implicit path (assembly, block-Jacobi / block-ILU(0) GMRES, CFL control)
+against the oracle and the reference's golden data.
+
+Tolerances: assembly (right-hand side and every 5x5 block) 1e-12 relative to the array's
+scale; per-step right-hand-side norms and CFL 1e-9 relative over the golden runs (the linear
+solve stops at 1e-2, so rounding differences of the order of 1e-15 in the system move the
+iterates by about that much and the adaptive CFL feeds them back); FP32 defect correction
+against the FP64 GPU solve: 1e-3 on the state after 20 steps.
+"""
+import numpy as np
+import pytest
+
+from bes_gb300 import meshgen
+from oracle import pyoracle
+from tests import _golden as G
+from tests._gpu import context, hist_rel_err, rel_err
+
+pytestmark = pytest.mark.gpu
+
+IMPLICIT = [c for c in G.CASES if c.startswith("implicit")]
+
+
+def implicit_opts(info, **extra):
+    m = info["meta"]
+    o = dict(solver_type=1, local_time_step=1 if m["local"] == "YES" else 0,
+             courant_num=float(m["cfl"]), adaptive_courant_num_max=float(m["cfl_max"]),
+             adaptive_courant_num_exponent=(1.0, 1.0), freestream_mach=tuple(m["mach"]),
+             linear_solver=1 if m["smoother"] == "ILU0" else 0,
+             linear_solver_tol=float(m["lin_tol"]), linear_solver_max_iter=int(m["lin_maxiter"]),
+             gmres_restart=30)
+    o.update(extra)
+    return o
+
+
+def _scalar_csr(blocks, rowptr_counts):
+    out = []
+    k = 0
+    for cnt in rowptr_counts:
+        for r in range(5):
+            for q in range(cnt):
+                out.append(blocks[k + q, r, :])
+        k += cnt
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("case", IMPLICIT)
+def test_assembly_matches_oracle_and_reference(case):
+    ref, info = G.load(case)
+    mesh = G.mesh_of(info)
+    ctx = context(mesh, **implicit_opts(info))
+    got = ctx.implicit_assemble(info["meta"]["cfl"])
+    O = pyoracle.Oracle(mesh, **G.oracle_kwargs(info))
+    exp = O.implicit_assemble(info["meta"]["cfl"])
+    assert rel_err(got["rhs"], exp["rhs"]) <= 1e-12
+    assert rel_err(got["blocks"], exp["vals"]) <= 1e-12
+    counts = np.diff(exp["rowptr"])
+    assert rel_err(got["rhs"], ref["op_rhs"]) <= 1e-12
+    assert rel_err(_scalar_csr(got["blocks"], counts), ref["op_mat_val"]) <= 1e-12
+
+
+@pytest.mark.parametrize("case", IMPLICIT)
+def test_implicit_history_matches_oracle(case):
+    ref, info = G.load(case)
+    mesh = G.mesh_of(info)
+    ctx = context(mesh, **implicit_opts(info))
+    n = info["steps"]
+    h = ctx.implicit_steps(n)
+    O = pyoracle.Oracle(mesh, **G.oracle_kwargs(info))
+    O.set_ilu_order(ctx.ilu_order())
+    ho = O.implicit_run(n)
+    assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
+    assert np.array_equal(h[:, 12], ho[:, 12])  # linear iterations
+    assert rel_err(ctx.get_state(), O.get_state()) <= 1e-9
+    if info["meta"]["smoother"] != "ILU0":
+        # block Jacobi does not depend on the ordering: also the reference's own run
+        refh = ref["implicit_history"].reshape(-1, 12)
+        assert hist_rel_err(h[:, :12], refh) <= 1e-9
+        assert rel_err(ctx.get_state(), ref["final_state"]) <= 1e-9
+
+
+def test_cfl_ramp_and_global_dt_match_oracle():
+    mesh = meshgen.gaussian_box(8, 4, 8)
+    mach = meshgen.freestream_mach_vector(0.7, 2.0, -1.0)
+    ctx = context(mesh, solver_type=1, local_time_step=0, courant_num=10.0,
+                  freestream_mach=mach, linear_solver=0, linear_solver_tol=1e-2,
+                  linear_solver_max_iter=200, cfl_ramp_steps=6, cfl_ramp_start=10.0,
+                  cfl_ramp_end=1000.0)
+    h = ctx.implicit_steps(8)
+    O = pyoracle.Oracle(mesh, solver=1, local_dt=0, cfl=10.0, mach=mach, lin_precond=0,
+                        lin_tol=1e-2, lin_maxiter=200, ramp_steps=6, ramp_cfl0=10.0,
+                        ramp_cfl1=1000.0)
+    ho = O.implicit_run(8)
+    expect_cfl = [10.0 * 100.0 ** (k / 5) for k in range(6)] + [1000.0, 1000.0]
+    assert np.allclose(h[:, 10], expect_cfl, rtol=1e-14)
+    assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+def test_fp32_defect_correction_tracks_fp64(precond):
+    mesh = meshgen.bump_channel(24, 8, 6, 0.08)
+    kw = dict(solver_type=1, local_time_step=1, courant_num=10.0, freestream_mach=(0.84, 0, 0),
+              linear_solver=precond, linear_solver_tol=1e-2, linear_solver_max_iter=300,
+              cfl_ramp_steps=10, cfl_ramp_start=10.0, cfl_ramp_end=200.0)
+    c64 = context(mesh, **kw)
+    c32 = context(mesh, precision=1, **kw)
+    h64 = c64.implicit_steps(20)
+    h32 = c32.implicit_steps(20)
+    assert rel_err(c32.get_state(), c64.get_state()) <= 1e-3
+    # the residual histories follow each other
+    assert np.max(np.abs(np.log(h32[:, :5] / h64[:, :5]))) <= 0.05
+    assert np.all(h32[:, 12] >= 1)
