@@ -70,7 +70,8 @@ def build(force: bool = False, verbose_ptxas: bool = False, quiet: bool = True) 
             for (s, _), out in zip(jobs, outs):
                 if out.strip():
                     print(f"== {os.path.basename(s)}\n{out}", file=sys.stderr)
-    if jobs or not os.path.exists(LIB):
+    if (jobs or not os.path.exists(LIB)
+            or max(os.path.getmtime(o) for o in objs) > os.path.getmtime(LIB)):
         tmp = LIB + f".tmp{os.getpid()}"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -419,6 +419,7 @@ int bes_explicit_enqueue(bes_ctx* ctx, int64_t n) {
       ctx->iters_since_reset = 0;
     }
     BES_CUDA_TRY(ctx, cudaGraphLaunch(ctx->it_graph[ctx->cur], ctx->stream));
+    ctx->launches += 2 + 3 * ctx->opt.n_stage;  // kernel nodes of one iteration graph
     ctx->cur ^= 1;
     ++ctx->iters_since_reset;
   }
@@ -448,6 +449,15 @@ int bes_last_kernel_times(bes_ctx* ctx, double* ms_out) {
   ms_out[1] = acc[1];
   ms_out[2] = acc[2];
   ms_out[3] = acc[0] + acc[1] + acc[2];
+  return BES_OK;
+}
+
+int bes_counters(const bes_ctx* ctx, int64_t* out) {
+  if (!ctx || !out) return BES_ERR_INVALID;
+  out[0] = ctx->launches;
+  out[1] = ctx->iterations_done;
+  out[2] = ctx->imp.step_count;
+  out[3] = ctx->imp.total_lin_iters;
   return BES_OK;
 }
 

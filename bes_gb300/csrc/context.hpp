@@ -68,6 +68,7 @@ struct ImplicitBuffers {
   double maxres_old[5] = {0, 0, 0, 0, 0};
   int64_t step_count = 0;
   int last_iters = 0;
+  int64_t total_lin_iters = 0;
   double last_err = 0;
 };
 }  // namespace bes
@@ -109,6 +110,7 @@ struct bes_ctx {
   int64_t iterations_done = 0;
   int64_t iters_since_reset = 0;  // graph launches since the history counter was reset
   bes::ImplicitBuffers imp;
+  int64_t launches = 0;  // kernels launched by this context (graph nodes counted per launch)
 };
 
 namespace bes {

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kBlock) update_kernel(
 }
 
 // One block: reduce the per-block partials in a fixed order into history[iter] (L2, max).
-__global__ void __launch_bounds__(kBlock) finalize_norms_kernel(
+static __global__ void __launch_bounds__(kBlock) finalize_norms_kernel(
     const double* __restrict__ partials, int nblocks, double* __restrict__ hist,
     int64_t hist_cap, int64_t* __restrict__ iter_ctr) {
   __shared__ double sh[kBlock / 32];
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(kBlock) finalize_norms_kernel(
   if (threadIdx.x == 0) *iter_ctr = it + 1;
 }
 
-__global__ void reset_dtmin_kernel(unsigned long long* dtmin) {
+static __global__ void reset_dtmin_kernel(unsigned long long* dtmin) {
   *dtmin = (unsigned long long)__double_as_longlong(1e300);
 }
 

@@ -72,6 +72,7 @@ struct Sys {
 int reduce_to_host(bes_ctx* c, int nrows, int nblocks, int nsum, int sqrt_sums, double* host) {
   reduce_rows_kernel<<<nrows, 256, 0, c->stream>>>(c->imp.red, nblocks, nsum, sqrt_sums,
                                                    c->imp.red_out);
+  ++c->launches;
   IMP_TRY(c, cudaMemcpyAsync(host, c->imp.red_out, nrows * sizeof(double), cudaMemcpyDeviceToHost,
                              c->stream));
   IMP_TRY(c, cudaStreamSynchronize(c->stream));
@@ -87,14 +88,17 @@ void precond_apply(const Sys<T>& S, const T* in, T* out) {
       const int n = M.color_off[k + 1] - M.color_off[k];
       ilu_lower_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
                                                          n, c->imp.ilu_pos, S.A, in, out);
+      ++S.c->launches;
     }
     for (int k = M.n_colors - 1; k >= 0; --k) {
       const int n = M.color_off[k + 1] - M.color_off[k];
       ilu_upper_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
                                                          n, c->imp.ilu_pos, S.A, S.Dinv, out);
+      ++S.c->launches;
     }
   } else {
     jacobi_apply_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, S.Dinv, in, out);
+    ++S.c->launches;
   }
 }
 
@@ -107,6 +111,7 @@ void precond_setup(const Sys<T>& S) {
     const int n = M.color_off[k + 1] - M.color_off[k];
     ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
                                                         n, c->imp.ilu_pos, S.A, S.Dinv);
+    ++S.c->launches;
   }
 }
 
@@ -120,18 +125,23 @@ int assemble(bes_ctx* c, double cfl, double* norms10) {
   const int local = o.local_time_step;
   double* U = c->U[c->cur];
   reset_dtmin_kernel<<<1, 1, 0, S.s>>>(c->dtmin);
+  ++S.c->launches;
   cell_recon_kernel<true, false><<<nblk(m.nc, kBlock), kBlock, 0, S.s>>>(
       m, c->prm, U, c->RS, c->rs_ld, c->dt, cfl, local, c->dtmin, nullptr, nullptr);
+  ++S.c->launches;
   face_flux_kernel<false><<<nblk(m.nf, kBlock), kBlock, 0, S.s>>>(m, c->prm, c->RS, c->rs_ld,
                                                                   c->FA, nullptr, c->nan_flag);
+  ++S.c->launches;
   FaceLocal fl{c->imp.m_own, c->imp.m_nb};
   face_jacobian_kernel<T><<<nblk(m.nf, 128), 128, 0, S.s>>>(
       m, c->prm, fl, U, c->dt, c->dtmin, local, o.jacobian_repeat, S.A, S.Dc);
+  ++S.c->launches;
   const int nb = nblk(m.nc, 128);
   cell_assemble_kernel<T><<<nb, 128, 0, S.s>>>(m, c->FA, c->dt, c->dtmin, local,
                                                o.jacobian_repeat, S.Dc, S.A,
                                                o.linear_solver == 1 ? nullptr : S.Dinv,
                                                c->imp.rhs, S.b, c->imp.red);
+  ++S.c->launches;
   IMP_TRY(c, cudaGetLastError());
   return reduce_to_host(c, 10, nb, 5, 1, norms10);
 }
@@ -148,7 +158,9 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
   const int G = kRedBlocks;
   double* red = c->imp.red;
   zero_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.N);
+  ++S.c->launches;
   norm2_kernel<T><<<G, 256, 0, S.s>>>(S.b, S.N, red);
+  ++S.c->launches;
   double norm_b2;
   int rc = reduce_to_host(c, 1, G, 1, 0, &norm_b2);
   if (rc) return rc;
@@ -162,30 +174,37 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
   double norm_r = norm_b;
   scale_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.b, 1.0, S.N);  // r = b
   double beta = norm_b;
+  ++S.c->launches;
   while (true) {
     if (beta < eps || iter >= maxiter) break;
     scale_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(0), S.W, 1.0 / beta, S.N);
+    ++S.c->launches;
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
     while (j < mr && iter < maxiter) {
       precond_apply(S, S.Vk(j), S.Z);
       spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.Z, nullptr, S.W);
+      ++S.c->launches;
       dots_kernel<T><<<G, 256, 0, S.s>>>(S.V, S.N, j + 1, S.W, S.N, red);
+      ++S.c->launches;
       if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h.data()))) return rc;
       IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h.data(), (j + 1) * sizeof(double),
                                  cudaMemcpyHostToDevice, S.s));
       axpy_reduce_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j + 1, c->imp.coef, S.N, 1, red);
+      ++S.c->launches;
       if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h2.data()))) return rc;
       IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h2.data(), (j + 1) * sizeof(double),
                                  cudaMemcpyHostToDevice, S.s));
       axpy_reduce_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j + 1, c->imp.coef, S.N, 2, red);
+      ++S.c->launches;
       double hn2;
       if ((rc = reduce_to_host(c, 1, G, 1, 0, &hn2))) return rc;
       for (int i = 0; i <= j; ++i) H[i * mr + j] = h[i] + h2[i];
       const double hn = std::sqrt(hn2);
       H[(j + 1) * mr + j] = hn;
       if (hn != 0.0) scale_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(j + 1), S.W, 1.0 / hn, S.N);
+      ++S.c->launches;
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * H[i * mr + j] + sn[i] * H[(i + 1) * mr + j];
         H[(i + 1) * mr + j] = -sn[i] * H[i * mr + j] + cs[i] * H[(i + 1) * mr + j];
@@ -210,10 +229,13 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
     }
     IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, S.s));
     lincomb_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j, c->imp.coef, S.N);
+    ++S.c->launches;
     precond_apply(S, S.W, S.Z);
     add_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.Z, S.N);
+    ++S.c->launches;
     spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.X, S.b, S.W);  // r = b - A x
     norm2_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.N, red);
+    ++S.c->launches;
     double nr2;
     if ((rc = reduce_to_host(c, 1, G, 1, 0, &nr2))) return rc;
     norm_r = std::sqrt(nr2);
@@ -255,6 +277,7 @@ int implicit_step(bes_ctx* c, double* hist14) {
   rc = gmres<T>(c, iters, rel);
   if (rc) return rc;
   state_update_kernel<T><<<kRedBlocks, 256, 0, c->stream>>>(c->U[c->cur], S.X, S.N);
+  ++c->launches;
   IMP_TRY(c, cudaGetLastError());
   for (int v = 0; v < 5; ++v) I.maxres[v] = norms[5 + v];
   if (o.cfl_ramp_steps <= 0 && o.adaptive_courant_num_max > o.courant_num) {
@@ -265,6 +288,7 @@ int implicit_step(bes_ctx* c, double* hist14) {
     I.cfl_actual = std::min(o.adaptive_courant_num_max, I.cfl_actual);
   }
   I.last_iters = iters;
+  I.total_lin_iters += iters;
   I.last_err = rel;
   if (hist14) {
     for (int k = 0; k < 10; ++k) hist14[k] = norms[k];

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(128) cell_assemble_kernel(
 
 // Reduce `nvals` rows of per-block partials (sums, or maxima for rows >= nsum) in a fixed
 // order; one block per value.  out[k] = sum (sqrt if sqrt_sums) or max.
-__global__ void __launch_bounds__(256) reduce_rows_kernel(const double* __restrict__ partials,
+static __global__ void __launch_bounds__(256) reduce_rows_kernel(const double* __restrict__ partials,
                                                           int nblocks, int nsum, int sqrt_sums,
                                                           double* __restrict__ out) {
   __shared__ double sh[8];

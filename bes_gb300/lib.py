@@ -26,7 +26,7 @@ EXPORTED = [
     "bes_flux_batch", "bes_build_info", "bes_abi_sizes", "bes_host_geometry",
     "bes_explicit_enqueue", "bes_synchronize", "bes_stream", "bes_last_kernel_times",
     "bes_residual_norms_static", "bes_implicit_steps", "bes_implicit_assemble",
-    "bes_ilu_order",
+    "bes_ilu_order", "bes_counters",
 ]
 
 
@@ -103,6 +103,7 @@ def load(path: str = LIB_PATH):
     L.bes_implicit_steps.argtypes = [P, ctypes.c_int64, D]
     L.bes_implicit_assemble.argtypes = [P, ctypes.c_double, D, D, ctypes.POINTER(ctypes.c_int64)]
     L.bes_ilu_order.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    L.bes_counters.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_residual_norms_static.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
     I64 = ctypes.POINTER(ctypes.c_int64)
@@ -318,6 +319,12 @@ class Context:
         self._check(load().bes_implicit_assemble(self.h, float(cfl), _d(rhs), _d(blocks),
                                                  ctypes.byref(nb)))
         return dict(rhs=rhs, blocks=blocks)
+
+    def counters(self) -> dict:
+        out = np.zeros(4, np.int64)
+        self._check(load().bes_counters(self.h, _i(out)))
+        return dict(launches=int(out[0]), explicit_iterations=int(out[1]),
+                    implicit_steps=int(out[2]), linear_iterations=int(out[3]))
 
     def ilu_order(self) -> np.ndarray:
         o = np.zeros(self.n_cells, np.int64)

@@ -177,6 +177,10 @@ int bes_last_kernel_times(bes_ctx* ctx, double* ms_out);
 int bes_residual_norms_static(const double* residual, int64_t n_cells, double* norms,
                               void* stream, char* err, size_t err_cap);
 
+/* Counters of the context: out[0] kernels launched (graph kernel nodes counted per graph
+ * launch), out[1] explicit iterations, out[2] implicit steps, out[3] linear iterations. */
+int bes_counters(const bes_ctx* ctx, int64_t* out);
+
 /* Library build identification (e.g. "sm_103a"). */
 const char* bes_build_info(void);
 
