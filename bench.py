@@ -281,6 +281,33 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
     return line
 
 
+def run_converge(args, wl, ctx, max_steps: int, drop: float = 1e-8):
+    """Implicit steps until the L2 of the unscaled residual (all variables) falls by `drop`
+    relative to the first step; returns steps, device-synchronous wall time and the history."""
+    import torch
+    hist = []
+    t0 = time.perf_counter()
+    r0 = None
+    steps = 0
+    for _ in range(max_steps):
+        h = ctx.implicit_steps(1)[0]
+        hist.append(h)
+        steps += 1
+        r = float(np.sqrt(np.sum(h[14:19] ** 2)))
+        if r0 is None:
+            r0 = r
+        if r <= drop * r0 or not np.isfinite(r):
+            break
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    hist = np.array(hist)
+    rel = float(np.sqrt(np.sum(hist[-1, 14:19] ** 2)) / r0)
+    return dict(steps=steps, seconds=dt, final_drop=rel, converged=bool(rel <= drop),
+                linear_iterations=int(hist[:, 12].sum()),
+                solves_per_hour=3600.0 / dt if rel <= drop else 0.0,
+                wall_force=[float(x) for x in ctx.wall_force()])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -289,6 +316,8 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="explicit_bump_72k", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--converge", type=int, default=0,
+                    help="implicit workloads: also solve to a 1e-8 residual drop (max steps)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -313,6 +342,11 @@ def main():
     nc, nf = ctx.n_cells, ctx.n_faces
     if wl["kind"] == "implicit":
         line = run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist)
+        if args.converge:
+            ctx.set_freestream_state()
+            ctx2 = lib.Context(mesh, lib.default_options(**wl["opts"]))
+            line["converged_solve"] = run_converge(args, wl, ctx2, args.converge)
+            ctx2.close()
         ctx.close()
         if rank == 0:
             print(json.dumps(line))

@@ -461,4 +461,27 @@ int bes_counters(const bes_ctx* ctx, int64_t* out) {
   return BES_OK;
 }
 
+int bes_wall_force(bes_ctx* ctx, double* force) {
+  if (!ctx || !force) return BES_ERR_INVALID;
+  // Integrated slip-wall pressure force sum_f p_owner S_f with the owner cell's pressure, the
+  // quantity of the reference's slip-wall output (SolutionSnapshot::writeSlipWallToCsv,
+  // src/SolutionSnapshot.cpp:268-309), in non-dimensional units, summed in face order.
+  const int64_t nc = ctx->soa.nc;
+  std::vector<double> U(5 * nc);
+  int rc = bes_get_state(ctx, U.data());
+  if (rc) return rc;
+  const RefMesh& R = ctx->ref;
+  const double gm1 = ctx->prm.gas.gm1;
+  double F[3] = {0, 0, 0};
+  for (int64_t f = 0; f < R.nf; ++f) {
+    if (R.kind[f] != KIND_SLIP_WALL) continue;
+    const double* u = &U[R.owner[f] * 5];
+    const double k = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
+    const double p = gm1 * (u[4] - k / (2.0 * u[0]));
+    for (int d = 0; d < 3; ++d) F[d] += p * R.S[f * 3 + d];
+  }
+  for (int d = 0; d < 3; ++d) force[d] = F[d];
+  return BES_OK;
+}
+
 }  // extern "C"

@@ -115,10 +115,10 @@ void precond_setup(const Sys<T>& S) {
   }
 }
 
-// Residual, first-order Jacobians and the assembled system at the current state; the FP64
-// right-hand side norms (L2[5], max[5]) are returned in norms10.
+// Residual, first-order Jacobians and the assembled system at the current state; returns the
+// FP64 norms: L2[5] and max[5] of the Dt/V-scaled right-hand side, L2[5] of the residual R.
 template <class T>
-int assemble(bes_ctx* c, double cfl, double* norms10) {
+int assemble(bes_ctx* c, double cfl, double* norms15) {
   Sys<T> S(c);
   const DevMesh& m = c->dm;
   const bes_options& o = c->opt;
@@ -143,7 +143,15 @@ int assemble(bes_ctx* c, double cfl, double* norms10) {
                                                c->imp.rhs, S.b, c->imp.red);
   ++S.c->launches;
   IMP_TRY(c, cudaGetLastError());
-  return reduce_to_host(c, 10, nb, 5, 1, norms10);
+  double r[15];
+  const int rc = reduce_to_host(c, 15, nb, 10, 1, r);
+  // norms15: L2 of the right-hand side [5], max of the right-hand side [5], L2 of R [5]
+  for (int v = 0; v < 5; ++v) {
+    norms15[v] = r[v];
+    norms15[5 + v] = r[10 + v];
+    norms15[10 + v] = r[5 + v];
+  }
+  return rc;
 }
 
 // Right-preconditioned GMRES(m), x0 = 0, classical Gram-Schmidt with one re-orthogonalisation
@@ -260,12 +268,12 @@ double cfl_for_step(const bes_ctx* c) {
 }
 
 template <class T>
-int implicit_step(bes_ctx* c, double* hist14) {
+int implicit_step(bes_ctx* c, double* hist) {
   ImplicitBuffers& I = c->imp;
   const bes_options& o = c->opt;
   for (int v = 0; v < 5; ++v) I.maxres_old[v] = I.maxres[v];
   const double cfl = cfl_for_step(c);
-  double norms[10];
+  double norms[15];
   int rc = assemble<T>(c, cfl, norms);
   if (rc) return rc;
   rc = check_nan_public(c);
@@ -290,12 +298,13 @@ int implicit_step(bes_ctx* c, double* hist14) {
   I.last_iters = iters;
   I.total_lin_iters += iters;
   I.last_err = rel;
-  if (hist14) {
-    for (int k = 0; k < 10; ++k) hist14[k] = norms[k];
-    hist14[10] = cfl;
-    hist14[11] = I.cfl_actual;
-    hist14[12] = iters;
-    hist14[13] = rel;
+  if (hist) {
+    for (int k = 0; k < 10; ++k) hist[k] = norms[k];
+    hist[10] = cfl;
+    hist[11] = I.cfl_actual;
+    hist[12] = iters;
+    hist[13] = rel;
+    for (int k = 0; k < 5; ++k) hist[14 + k] = norms[10 + k];
   }
   ++I.step_count;
   return BES_OK;
@@ -354,8 +363,8 @@ int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history) {
     return BES_ERR_INVALID;
   }
   for (int64_t i = 0; i < n; ++i) {
-    int rc = ctx->imp.prec ? implicit_step<float>(ctx, history ? history + i * 14 : nullptr)
-                           : implicit_step<double>(ctx, history ? history + i * 14 : nullptr);
+    int rc = ctx->imp.prec ? implicit_step<float>(ctx, history ? history + i * 19 : nullptr)
+                           : implicit_step<double>(ctx, history ? history + i * 19 : nullptr);
     if (rc) return rc;
   }
   IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -375,7 +384,7 @@ int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks,
   }
   if (n_blocks) *n_blocks = nb;
   if (!rhs && !blocks) return BES_OK;
-  double norms[10];
+  double norms[15];
   int rc = ctx->imp.prec ? assemble<float>(ctx, cfl, norms) : assemble<double>(ctx, cfl, norms);
   if (rc) return rc;
   IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));

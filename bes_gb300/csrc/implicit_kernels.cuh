@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(128) cell_assemble_kernel(
   const int nc = m.nc, nf = m.nf;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double b[5] = {0, 0, 0, 0, 0};
+  double R[5] = {0, 0, 0, 0, 0};  // unscaled residual sum(+-F A), for convergence monitoring
   if (i < nc) {
     const double dti = local_dt ? dt[i] : __longlong_as_double((long long)*dtmin);
     const double k = dti * m.inv_vol[i];
@@ -174,8 +175,10 @@ __global__ void __launch_bounds__(128) cell_assemble_kernel(
       const int f = gf >= 0 ? gf : ~gf;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const double x = k * FA[(int64_t)v * nf + f];
+        const double fa = FA[(int64_t)v * nf + f];
+        const double x = k * fa;
         b[v] = gf >= 0 ? b[v] - x : b[v] + x;
+        R[v] = gf >= 0 ? R[v] + fa : R[v] - fa;
       }
       const T* src = Dc + (gf >= 0 ? 0 : (int64_t)25 * nf);
 #pragma unroll
@@ -198,24 +201,28 @@ __global__ void __launch_bounds__(128) cell_assemble_kernel(
       rhs_t[(int64_t)v * nc + i] = (T)b[v];
     }
   }
-  __shared__ double sh[10][4];
+  __shared__ double sh[15][4];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     const double s2 = warp_sum(b[v] * b[v]);
     const double mx = warp_max(fabs(b[v]));
+    const double r2 = warp_sum(R[v] * R[v]);
     if (lane == 0) {
       sh[v][wid] = s2;
       sh[5 + v][wid] = mx;
+      sh[10 + v][wid] = r2;
     }
   }
   __syncthreads();
   if (threadIdx.x < 32) {
 #pragma unroll
-    for (int q = 0; q < 10; ++q) {
+    for (int q = 0; q < 15; ++q) {
       double x = lane < 4 ? sh[q][lane] : 0.0;
-      x = q < 5 ? warp_sum(x) : warp_max(x);
-      if (lane == 0) partials[(int64_t)q * gridDim.x + blockIdx.x] = x;
+      x = (q >= 5 && q < 10) ? warp_max(x) : warp_sum(x);
+      // rows: 0-4 sum b^2, 5-9 max |b|, 10-14 sum R^2
+      const int row = q < 5 ? q : (q < 10 ? q + 5 : q - 5);
+      if (lane == 0) partials[(int64_t)row * gridDim.x + blockIdx.x] = x;
     }
   }
 }

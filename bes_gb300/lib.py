@@ -26,7 +26,7 @@ EXPORTED = [
     "bes_flux_batch", "bes_build_info", "bes_abi_sizes", "bes_host_geometry",
     "bes_explicit_enqueue", "bes_synchronize", "bes_stream", "bes_last_kernel_times",
     "bes_residual_norms_static", "bes_implicit_steps", "bes_implicit_assemble",
-    "bes_ilu_order", "bes_counters",
+    "bes_ilu_order", "bes_counters", "bes_wall_force",
 ]
 
 
@@ -104,6 +104,7 @@ def load(path: str = LIB_PATH):
     L.bes_implicit_assemble.argtypes = [P, ctypes.c_double, D, D, ctypes.POINTER(ctypes.c_int64)]
     L.bes_ilu_order.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_counters.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    L.bes_wall_force.argtypes = [P, D]
     L.bes_residual_norms_static.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
     I64 = ctypes.POINTER(ctypes.c_int64)
@@ -306,8 +307,8 @@ class Context:
         return dict(cell_ms=ms[0], face_ms=ms[1], update_ms=ms[2], total_ms=ms[3])
 
     def implicit_steps(self, n: int):
-        """n implicit steps; history [n, 14] (see bes_implicit_steps)."""
-        h = np.zeros((n, 14))
+        """n implicit steps; history [n, 19] (see bes_implicit_steps)."""
+        h = np.zeros((n, 19))
         self._check(load().bes_implicit_steps(self.h, int(n), _d(h)))
         return h
 
@@ -319,6 +320,11 @@ class Context:
         self._check(load().bes_implicit_assemble(self.h, float(cfl), _d(rhs), _d(blocks),
                                                  ctypes.byref(nb)))
         return dict(rhs=rhs, blocks=blocks)
+
+    def wall_force(self) -> np.ndarray:
+        f = np.zeros(3)
+        self._check(load().bes_wall_force(self.h, _d(f)))
+        return f
 
     def counters(self) -> dict:
         out = np.zeros(4, np.int64)

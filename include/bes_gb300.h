@@ -128,9 +128,10 @@ int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
  * colour-ordered block-ILU(0) (linear_solver 1) preconditioner, in FP64 (precision 0) or FP32
  * (precision 1, defect correction: residual, update and norms stay FP64), the update, and the
  * CFL control (adaptive as adaptCourantNum_, src/SolverImplicit.cpp:530-550, or the additive
- * geometric ramp).  history (may be NULL): [n][14] = L2[5] and max[5] of the Dt/V-scaled
+ * geometric ramp).  history (may be NULL): [n][19] = L2[5] and max[5] of the Dt/V-scaled
  * right-hand side (the max is what the reference logs, Q10), CFL used, CFL after the step,
- * linear iterations, final relative linear residual. */
+ * linear iterations, final relative linear residual, L2[5] of the unscaled residual
+ * R = sum(+-F A) (the convergence measure). */
 int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history);
 
 /* Assemble (without solving or updating) the implicit system at the current state and CFL
@@ -176,6 +177,11 @@ int bes_last_kernel_times(bes_ctx* ctx, double* ms_out);
  * calls that overlap on the GPU race.  Returns after enqueueing (does not synchronise). */
 int bes_residual_norms_static(const double* residual, int64_t n_cells, double* norms,
                               void* stream, char* err, size_t err_cap);
+
+/* Integrated slip-wall pressure force F = sum over slip-wall faces of p S (owner-cell
+ * pressure, dimensional face normal S, non-dimensional units), the quantity behind the
+ * reference's slip-wall output (src/SolutionSnapshot.cpp:268-309).  force [3]. */
+int bes_wall_force(bes_ctx* ctx, double* force);
 
 /* Counters of the context: out[0] kernels launched (graph kernel nodes counted per graph
  * launch), out[1] explicit iterations, out[2] implicit steps, out[3] linear iterations. */

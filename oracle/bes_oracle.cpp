@@ -624,6 +624,23 @@ static void implicit_step(Oracle& O, double* hist) {
       hist[5 + v] = O.maxres[v];
     }
     hist[10] = cfl;
+    // L2 of the unscaled residual R = sum(+-F A), summed per cell in increasing face id
+    double r2[5] = {0, 0, 0, 0, 0};
+    for (int64_t c = 0; c < M.nc; ++c) {
+      double R[5] = {0, 0, 0, 0, 0};
+      for (int q = 0; q < 4; ++q) {
+        const int m = (int)O.cface_sorted[c * 4 + q];
+        const int64_t f = M.cface[c * 4 + m];
+        for (int v = 0; v < 5; ++v) {
+          if (M.owner[f] == c)
+            R[v] += O.F[f * 5 + v] * M.area[f];
+          else
+            R[v] -= O.F[f * 5 + v] * M.area[f];
+        }
+      }
+      for (int v = 0; v < 5; ++v) r2[v] += R[v] * R[v];
+    }
+    for (int v = 0; v < 5; ++v) hist[12 + v] = std::sqrt(r2[v]);
   }
   if (O.o.ramp_steps <= 0 && O.o.cfl_max > O.o.cfl) {  // adaptCourantNum_
     const int idx = (O.maxres_old[0] > O.maxres[0]) ? 1 : 0;
@@ -777,18 +794,19 @@ void bor_set_ilu_order(void* h, const int64_t* order) {
   O->ilu_order.assign(order, order + O->M.nc);
 }
 
-// n implicit steps; hist [n*14] = L2[5] and max[5] of the Dt/V-scaled RHS, CFL used,
-// CFL after adaptation, linear iterations, linear relative residual.
+// n implicit steps; hist [n*19] = L2[5] and max[5] of the Dt/V-scaled RHS, CFL used,
+// CFL after adaptation, linear iterations, linear relative residual, L2[5] of R.
 void bor_implicit_run(void* h, int64_t n, double* hist) {
   bor::Oracle* O = static_cast<bor::Oracle*>(h);
   if (O->A.n == 0) bor::build_pattern(*O);
   for (int64_t i = 0; i < n; ++i) {
-    double loc[12];
+    double loc[17];
     bor::implicit_step(*O, loc);
     if (hist) {
-      std::memcpy(&hist[i * 14], loc, sizeof(loc));
-      hist[i * 14 + 12] = O->last_lin_iters;
-      hist[i * 14 + 13] = O->last_lin_err;
+      std::memcpy(&hist[i * 19], loc, 12 * sizeof(double));
+      hist[i * 19 + 12] = O->last_lin_iters;
+      hist[i * 19 + 13] = O->last_lin_err;
+      for (int v = 0; v < 5; ++v) hist[i * 19 + 14 + v] = loc[12 + v];
     }
   }
 }
@@ -810,7 +828,7 @@ int64_t bor_implicit_assemble(void* h, double cfl, double* rhs, double* vals, in
   std::memcpy(mro, O->maxres_old, sizeof(mro));
   const int lp = O->o.lin_maxiter;
   O->o.lin_maxiter = 0;
-  double loc[12];
+  double loc[17];
   bor::implicit_step(*O, loc);
   O->o.lin_maxiter = lp;
   O->Un = U0;

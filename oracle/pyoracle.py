@@ -186,7 +186,7 @@ class Oracle:
         lib().bor_set_ilu_order(self.h, _i(order))
 
     def implicit_run(self, n: int) -> np.ndarray:
-        h = np.zeros((n, 14))
+        h = np.zeros((n, 19))
         lib().bor_implicit_run(self.h, int(n), _d(h))
         return h
 

@@ -23,5 +23,15 @@ def rel_err(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
-def hist_rel_err(h, ref):
-    return np.max(np.abs(h - ref) / np.maximum(np.abs(ref), 1e-300))
+def hist_rel_err(h, ref, floor=1e-9):
+    """Largest relative difference of two norm histories ([steps, k]).  Each entry is compared
+    relative to itself, but never to less than `floor` times the largest norm of the same
+    group of five (L2 or max) in that step: a variable whose residual is pure rounding noise
+    (e.g. the spanwise momentum of a 2-D flow) has no meaningful relative error."""
+    h = np.asarray(h, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = np.abs(ref).copy()
+    for g0 in range(0, min(ref.shape[1], 10), 5):
+        grp = np.abs(ref[:, g0:g0 + 5]).max(axis=1, keepdims=True)
+        scale[:, g0:g0 + 5] = np.maximum(scale[:, g0:g0 + 5], floor * grp)
+    return np.max(np.abs(h - ref) / np.maximum(scale, 1e-300))

@@ -69,6 +69,7 @@ def test_implicit_history_matches_oracle(case):
     O.set_ilu_order(ctx.ilu_order())
     ho = O.implicit_run(n)
     assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
+    assert hist_rel_err(h[:, 14:19], ho[:, 14:19]) <= 1e-9  # unscaled residual L2
     assert np.array_equal(h[:, 12], ho[:, 12])  # linear iterations
     assert rel_err(ctx.get_state(), O.get_state()) <= 1e-9
     if info["meta"]["smoother"] != "ILU0":
