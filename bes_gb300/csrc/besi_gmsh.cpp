@@ -140,13 +140,10 @@ extern "C" int bes_options_from_besi(const char* path, bes_options* o, char* mes
     } else if (key == "SAVE_INTERVAL") {
       if (!num(0, x)) return bad("bad SAVE_INTERVAL");
     } else if (key == "FREESTREAM_RAMP") {
-      if (!num(0, x)) return bad("bad FREESTREAM_RAMP");
-      if (x > 0) {
-        set_err(err, err_cap, "FREESTREAM_RAMP > 0 is not implemented by this library");
-        return BES_ERR_UNSUPPORTED;
-      }
+      if (!num(0, x) || x < 0) return bad("bad FREESTREAM_RAMP");
+      o->freestream_ramp = (int32_t)x;
     } else if (key == "FREESTREAM_RAMP_START_FRAC") {
-      if (!num(0, x)) return bad("bad FREESTREAM_RAMP_START_FRAC");
+      if (!num(0, o->freestream_ramp_start_frac)) return bad("bad FREESTREAM_RAMP_START_FRAC");
     } else if (key == "GRADIENT_SCHEME") {
       if (word({"GREEN_GAUSS"}) < 0) return bad("Gradient scheme not supported");
     } else if (key == "LIMITER_SCHEME") {

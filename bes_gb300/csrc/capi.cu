@@ -78,7 +78,7 @@ void enqueue_iteration(bes_ctx* ctx, int cur) {
   double* Uk = ctx->U[cur ^ 1];
   const int local = o.local_time_step;
   cudaStream_t s = ctx->stream;
-  reset_dtmin_kernel<<<1, 1, 0, s>>>(ctx->dtmin);
+  freestream_step_kernel<<<1, 1, 0, s>>>(ctx->prm, ctx->step_dev, ctx->pinf_dev, ctx->dtmin);
   for (int k = 0; k < o.n_stage; ++k) {
     cudaEvent_t* e = ctx->kev[k];
     const double* Uin = (k == 0) ? Un : Uk;
@@ -234,6 +234,8 @@ int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** ou
   rc |= dev_alloc(c, &c->hist, 10 * c->hist_cap);
   rc |= dev_alloc(c, &c->iter_ctr, 1);
   rc |= dev_alloc(c, &c->nan_flag, 1);
+  rc |= dev_alloc(c, &c->pinf_dev, 6);
+  rc |= dev_alloc(c, &c->step_dev, 1);
   if (rc) return BES_ERR_CUDA;
   BES_CUDA_TRY(c, cudaMemset(c->iter_ctr, 0, sizeof(int64_t)));
   BES_CUDA_TRY(c, cudaMemset(c->nan_flag, 0, sizeof(int)));
@@ -243,6 +245,9 @@ int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** ou
   for (int d = 0; d < 3; ++d) c->prm.pinf[1 + d] = opt->freestream_mach[d];
   c->prm.pinf[4] = 1.0 / opt->specific_heat_ratio;
   c->prm.pinf[5] = 1.0 / (opt->specific_heat_ratio * opt->gas_constant);
+  c->prm.pinf_dev = c->pinf_dev;
+  c->prm.ramp_steps = opt->freestream_ramp;
+  c->prm.ramp_frac = opt->freestream_ramp_start_frac;
   rc = build_graphs(c);
   if (rc) return rc;
   if (opt->solver_type == 1) {
@@ -279,8 +284,18 @@ int bes_sizes(const bes_ctx* ctx, int64_t* n_cells, int64_t* n_faces) {
 
 int bes_set_freestream_state(bes_ctx* ctx) {
   if (!ctx) return BES_ERR_INVALID;
-  // GasPerfect_::computeAllConservedVariable of the freestream primitives (:182-216)
-  const double* P = ctx->prm.pinf;
+  // A new solve: step counter, CFL control and freestream ramp restart at step 0.
+  ctx->host_step = 0;
+  ctx->imp.step_count = 0;
+  ctx->imp.cfl_actual = ctx->opt.courant_num;
+  for (int v = 0; v < 5; ++v) ctx->imp.maxres[v] = ctx->imp.maxres_old[v] = 0.0;
+  const int64_t zero = 0;
+  BES_CUDA_TRY(ctx, cudaMemcpy(ctx->step_dev, &zero, sizeof(zero), cudaMemcpyHostToDevice));
+  // GasPerfect_::computeAllConservedVariable of the step-0 freestream primitives
+  // (:182-216; setUniversalInitialCondition gets getFreestreamPrimitiveVariables(0))
+  double P[6];
+  freestream_at(ctx->prm, 0, P);
+  BES_CUDA_TRY(ctx, cudaMemcpy(ctx->pinf_dev, P, sizeof(P), cudaMemcpyHostToDevice));
   double Uf[5];
   Uf[0] = P[0];
   double s = 0;
@@ -359,6 +374,9 @@ int bes_compute_operators(bes_ctx* ctx, double cfl, double* dt, double* grad, do
   const DevMesh& m = c->dm;
   double* Ucur = c->U[c->cur];
   double* scratch = c->U[c->cur ^ 1];
+  double P[6];
+  freestream_at(c->prm, c->host_step, P);
+  BES_CUDA_TRY(c, cudaMemcpyAsync(c->pinf_dev, P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
   reset_dtmin_kernel<<<1, 1, 0, c->stream>>>(c->dtmin);
   cell_recon_kernel<true, true><<<blocks_for(nc), kBlock, 0, c->stream>>>(
       m, c->prm, Ucur, c->RS, c->rs_ld, c->dt, cfl, 1, c->dtmin, c->G, c->PHI);
@@ -420,6 +438,7 @@ int bes_explicit_enqueue(bes_ctx* ctx, int64_t n) {
     }
     BES_CUDA_TRY(ctx, cudaGraphLaunch(ctx->it_graph[ctx->cur], ctx->stream));
     ctx->launches += 2 + 3 * ctx->opt.n_stage;  // kernel nodes of one iteration graph
+    ++ctx->host_step;
     ctx->cur ^= 1;
     ++ctx->iters_since_reset;
   }

@@ -27,8 +27,21 @@ struct DevMesh {
 
 struct Params {
   GasConst gas;
-  double pinf[6];  // freestream primitives (rho, u, v, w, p, T), Config.cpp:480-488
+  double pinf[6];        // freestream primitives (rho, u, v, w, p, T), Config.cpp:480-488
+  const double* pinf_dev;  // the current step's freestream primitives (device, ramped)
+  int32_t ramp_steps;      // FREESTREAM_RAMP
+  double ramp_frac;        // FREESTREAM_RAMP_START_FRAC
 };
+
+// Freestream primitives of step t (Config::getFreestreamPrimitiveVariables,
+// src/Config.cpp:688-706): the velocity ramps from frac * u_inf to u_inf over ramp_steps.
+BES_HD void freestream_at(const Params& p, int64_t t, double* out) {
+  for (int i = 0; i < 6; ++i) out[i] = p.pinf[i];
+  if (p.ramp_steps > 0 && t < p.ramp_steps) {
+    const double s = p.ramp_frac + (double)t / (double)p.ramp_steps * (1 - p.ramp_frac);
+    for (int d = 0; d < 3; ++d) out[1 + d] = p.pinf[1 + d] * s;
+  }
+}
 
 template <class T>
 struct DevBuf {
@@ -47,7 +60,8 @@ namespace bes {
 struct ImplicitBuffers {
   int prec = 0;          // 0: FP64 system, 1: FP32 system (defect correction)
   size_t tsize = 8;      // sizeof(T)
-  void* A = nullptr;     // ELL blocks [5 slots][25][nc] (factorised in place for ILU)
+  void* A = nullptr;     // ELL blocks [5 slots][25][nc]
+  void* LU = nullptr;    // block-ILU(0) factors in the same layout (ILU only)
   void* Dinv = nullptr;  // [25][nc] inverse diagonal (Jacobi) / inverse U_ii (ILU)
   void* Dc = nullptr;    // per-face diagonal contributions [2][25][nf]
   void* b = nullptr;     // right-hand side in T [5][nc]
@@ -102,6 +116,9 @@ struct bes_ctx {
   int64_t hist_cap = 0;
   int64_t* iter_ctr = nullptr;
   int* nan_flag = nullptr;  // face index + 1 of a NaN flux (0 none)
+  double* pinf_dev = nullptr;     // [6] freestream primitives of the current step
+  int64_t* step_dev = nullptr;    // solver step counter read by the explicit graphs
+  int64_t host_step = 0;          // the same counter on the host
   // graphs: one explicit iteration for each parity of the current snapshot
   cudaGraphExec_t it_graph[2] = {nullptr, nullptr};
   // event pairs around every kernel of an explicit iteration (graph event-record nodes):

@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kBlock) face_flux_kernel(
   } else if (f < m.nf_int + m.nf_slip) {
     slipwall_flux(prm.gas, UL, n, F);
   } else {
-    freestream_flux(prm.gas, UL, prm.pinf, n, F);
+    freestream_flux(prm.gas, UL, prm.pinf_dev, n, F);
   }
   const double A = m.farea[f];
   bool bad = false;
@@ -310,6 +310,16 @@ static __global__ void __launch_bounds__(kBlock) finalize_norms_kernel(
 }
 
 static __global__ void reset_dtmin_kernel(unsigned long long* dtmin) {
+  *dtmin = (unsigned long long)__double_as_longlong(1e300);
+}
+
+// First node of an explicit iteration: the freestream of this step, then the step counter.
+static __global__ void freestream_step_kernel(Params prm, int64_t* step, double* pinf_dev,
+                                              unsigned long long* dtmin) {
+  double p[6];
+  freestream_at(prm, *step, p);
+  for (int i = 0; i < 6; ++i) pinf_dev[i] = p[i];
+  *step += 1;
   *dtmin = (unsigned long long)__double_as_longlong(1e300);
 }
 

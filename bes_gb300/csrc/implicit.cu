@@ -43,6 +43,7 @@ struct Sys {
   int nc;
   int64_t N;
   T* A;
+  T* LU;
   T* Dinv;
   T* Dc;
   T* b;
@@ -56,6 +57,7 @@ struct Sys {
     nc = ctx->soa.nc;
     N = 5LL * nc;
     A = (T*)I.A;
+    LU = (T*)I.LU;
     Dinv = (T*)I.Dinv;
     Dc = (T*)I.Dc;
     b = (T*)I.b;
@@ -87,13 +89,13 @@ void precond_apply(const Sys<T>& S, const T* in, T* out) {
     for (int k = 0; k < M.n_colors; ++k) {
       const int n = M.color_off[k + 1] - M.color_off[k];
       ilu_lower_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
-                                                         n, c->imp.ilu_pos, S.A, in, out);
+                                                         n, c->imp.ilu_pos, S.LU, in, out);
       ++S.c->launches;
     }
     for (int k = M.n_colors - 1; k >= 0; --k) {
       const int n = M.color_off[k + 1] - M.color_off[k];
       ilu_upper_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
-                                                         n, c->imp.ilu_pos, S.A, S.Dinv, out);
+                                                         n, c->imp.ilu_pos, S.LU, S.Dinv, out);
       ++S.c->launches;
     }
   } else {
@@ -107,10 +109,12 @@ void precond_setup(const Sys<T>& S) {
   bes_ctx* c = S.c;
   const SoaMesh& M = c->soa;
   if (c->opt.linear_solver != 1) return;  // block Jacobi inverted during assembly
+  // the factors overwrite a copy: the Krylov products need the unfactored matrix
+  cudaMemcpyAsync(S.LU, S.A, (size_t)125 * S.nc * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
   for (int k = 0; k < M.n_colors; ++k) {
     const int n = M.color_off[k + 1] - M.color_off[k];
     ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
-                                                        n, c->imp.ilu_pos, S.A, S.Dinv);
+                                                        n, c->imp.ilu_pos, S.LU, S.Dinv);
     ++S.c->launches;
   }
 }
@@ -194,17 +198,17 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       precond_apply(S, S.Vk(j), S.Z);
       spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.Z, nullptr, S.W);
       ++S.c->launches;
-      dots_kernel<T><<<G, 256, 0, S.s>>>(S.V, S.N, j + 1, S.W, S.N, red);
+      launch_dots<T>(j + 1, G, S.s, S.V, S.N, S.W, S.N, red);
       ++S.c->launches;
       if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h.data()))) return rc;
       IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h.data(), (j + 1) * sizeof(double),
                                  cudaMemcpyHostToDevice, S.s));
-      axpy_reduce_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j + 1, c->imp.coef, S.N, 1, red);
+      launch_axpy<T>(j + 1, true, G, S.s, S.W, S.V, S.N, c->imp.coef, S.N, red);
       ++S.c->launches;
       if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h2.data()))) return rc;
       IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h2.data(), (j + 1) * sizeof(double),
                                  cudaMemcpyHostToDevice, S.s));
-      axpy_reduce_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j + 1, c->imp.coef, S.N, 2, red);
+      launch_axpy<T>(j + 1, false, G, S.s, S.W, S.V, S.N, c->imp.coef, S.N, red);
       ++S.c->launches;
       double hn2;
       if ((rc = reduce_to_host(c, 1, G, 1, 0, &hn2))) return rc;
@@ -273,6 +277,9 @@ int implicit_step(bes_ctx* c, double* hist) {
   const bes_options& o = c->opt;
   for (int v = 0; v < 5; ++v) I.maxres_old[v] = I.maxres[v];
   const double cfl = cfl_for_step(c);
+  double P[6];
+  freestream_at(c->prm, c->host_step, P);  // FREESTREAM_RAMP
+  IMP_TRY(c, cudaMemcpyAsync(c->pinf_dev, P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
   double norms[15];
   int rc = assemble<T>(c, cfl, norms);
   if (rc) return rc;
@@ -307,6 +314,7 @@ int implicit_step(bes_ctx* c, double* hist) {
     for (int k = 0; k < 5; ++k) hist[14 + k] = norms[10 + k];
   }
   ++I.step_count;
+  ++c->host_step;
   return BES_OK;
 }
 
@@ -317,8 +325,8 @@ namespace bes {
 int implicit_allocate(bes_ctx* c) {
   ImplicitBuffers& I = c->imp;
   const bes_options& o = c->opt;
-  if (o.gmres_restart < 1 || o.gmres_restart > 31) {
-    c->last_error = "GMRES_RESTART must be between 1 and 31";
+  if (o.gmres_restart < 1 || o.gmres_restart > 32) {
+    c->last_error = "GMRES_RESTART must be between 1 and 32";
     return BES_ERR_UNSUPPORTED;
   }
   I.prec = o.precision ? 1 : 0;
@@ -328,6 +336,7 @@ int implicit_allocate(bes_ctx* c) {
   int rc = 0;
   rc |= imp_malloc(c, &I.A, 125 * nc * I.tsize);
   rc |= imp_malloc(c, &I.Dinv, 25 * nc * I.tsize);
+  if (o.linear_solver == 1) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
   rc |= imp_malloc(c, &I.b, N * I.tsize);
   rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * N * I.tsize);

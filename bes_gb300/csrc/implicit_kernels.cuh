@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(128) face_jacobian_kernel(
     else if (f < m.nf_int + m.nf_slip)
       slipwall_flux(g, dl, n, dfl);
     else
-      freestream_flux(g, dl, prm.pinf, n, dfl);
+      freestream_flux(g, dl, prm.pinf_dev, n, dfl);
     T* J = side == 0 ? JL : JR;
 #pragma unroll
     for (int a = 0; a < 5; ++a)
@@ -440,64 +440,113 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restric
     y[(int64_t)r * nc + i] = b ? b[(int64_t)r * nc + i] - acc[r] : acc[r];
 }
 
-// partial dots: partials[k*G + blk] = sum V_k . w over the block's grid-stride range
-template <class T>
-__global__ void __launch_bounds__(256) dots_kernel(const T* __restrict__ V, int64_t ldv, int nvec,
-                                                   const T* __restrict__ w, int64_t N,
-                                                   double* __restrict__ partials) {
-  __shared__ double sh[8];
-  for (int k = 0; k < nvec; ++k) {
-    const T* vk = V + (int64_t)k * ldv;
+// Block reduction of NV per-thread double accumulators; partials[k*gridDim + blk].
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&acc)[NV], double* partials) {
+  __shared__ double sh[NV][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const double s = warp_sum(acc[k]);
+    if (lane == 0) sh[k][wid] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < NV; k += blockDim.x) {
     double s = 0.0;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
-         idx += (int64_t)gridDim.x * blockDim.x)
-      s += (double)vk[idx] * (double)w[idx];
-    s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      double x = threadIdx.x < 8 ? sh[threadIdx.x] : 0.0;
-      x = warp_sum(x);
-      if (threadIdx.x == 0) partials[(int64_t)k * gridDim.x + blockIdx.x] = x;
-    }
-    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += sh[k][q];
+    partials[(int64_t)k * gridDim.x + blockIdx.x] = s;
   }
 }
 
-// w -= sum_k h_k V_k; then (mode 1) partial dots V_k . w_new, or (mode 2) partial |w_new|^2
-template <class T>
-__global__ void __launch_bounds__(256) axpy_reduce_kernel(T* __restrict__ w, const T* __restrict__ V,
-                                                          int64_t ldv, int nvec,
-                                                          const double* __restrict__ h, int64_t N,
-                                                          int mode, double* __restrict__ partials) {
-  __shared__ double sh[32][8];
-  __shared__ double hs[64];
-  for (int k = threadIdx.x; k < nvec; k += blockDim.x) hs[k] = h[k];
-  __syncthreads();
-  double acc[32];
-  const int nacc = mode == 1 ? nvec : 1;
-  for (int k = 0; k < nacc; ++k) acc[k] = 0.0;
+// Partial dot products V_k . w for k < NV in one pass over the vectors (each element of w
+// and of every V_k is read once).
+template <class T, int NV>
+__global__ void __launch_bounds__(256) dots_kernel(const T* __restrict__ V, int64_t ldv,
+                                                   const T* __restrict__ w, int64_t N,
+                                                   double* __restrict__ partials) {
+  double acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x) {
+    const double wv = (double)w[idx];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] += (double)V[(int64_t)k * ldv + idx] * wv;
+  }
+  block_reduce_store<NV>(acc, partials);
+}
+
+// w -= sum_k h_k V_k (k < NV) in one pass; then DOTS: partial V_k . w_new, or else partial
+// |w_new|^2 (row 0).  Every element of w and of every V_k is read once.
+template <class T, int NV, bool DOTS>
+__global__ void __launch_bounds__(256) axpy_reduce_kernel(T* __restrict__ w, const T* __restrict__ V,
+                                                          int64_t ldv, const double* __restrict__ h,
+                                                          int64_t N, double* __restrict__ partials) {
+  double hs[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) hs[k] = h[k];
+  constexpr int NA = DOTS ? NV : 1;
+  double acc[NA];
+#pragma unroll
+  for (int k = 0; k < NA; ++k) acc[k] = 0.0;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    T v[NV];
     double x = (double)w[idx];
-    for (int k = 0; k < nvec; ++k) x -= hs[k] * (double)V[(int64_t)k * ldv + idx];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      v[k] = V[(int64_t)k * ldv + idx];
+      x -= hs[k] * (double)v[k];
+    }
     const T xt = (T)x;
     w[idx] = xt;
-    if (mode == 1) {
-      for (int k = 0; k < nvec; ++k) acc[k] += (double)V[(int64_t)k * ldv + idx] * (double)xt;
+    if (DOTS) {
+#pragma unroll
+      for (int k = 0; k < NA; ++k) acc[k] += (double)v[k] * (double)xt;
     } else {
       acc[0] += (double)xt * (double)xt;
     }
   }
-  for (int k = 0; k < nacc; ++k) {
-    const double s = warp_sum(acc[k]);
-    if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = s;
+  block_reduce_store<NA>(acc, partials);
+}
+
+// Launch helpers dispatching the vector count to a compile-time constant (1..32).
+#define BES_NV_CASES(X) \
+  X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) \
+  X(17) X(18) X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27) X(28) X(29) X(30) X(31) X(32)
+
+template <class T>
+void launch_dots(int nvec, int G, cudaStream_t s, const T* V, int64_t ldv, const T* w, int64_t N,
+                 double* partials) {
+  switch (nvec) {
+#define BES_DOTS_CASE(n) \
+  case n: dots_kernel<T, n><<<G, 256, 0, s>>>(V, ldv, w, N, partials); break;
+    BES_NV_CASES(BES_DOTS_CASE)
+#undef BES_DOTS_CASE
+    default: break;
   }
-  __syncthreads();
-  for (int k = threadIdx.x; k < nacc; k += blockDim.x) {
-    double s = 0.0;
-    for (int q = 0; q < 8; ++q) s += sh[k][q];
-    partials[(int64_t)k * gridDim.x + blockIdx.x] = s;
+}
+
+template <class T>
+void launch_axpy(int nvec, bool dots, int G, cudaStream_t s, T* w, const T* V, int64_t ldv,
+                 const double* h, int64_t N, double* partials) {
+  if (dots) {
+    switch (nvec) {
+#define BES_AXPY_CASE(n) \
+  case n: axpy_reduce_kernel<T, n, true><<<G, 256, 0, s>>>(w, V, ldv, h, N, partials); break;
+      BES_NV_CASES(BES_AXPY_CASE)
+#undef BES_AXPY_CASE
+      default: break;
+    }
+  } else {
+    switch (nvec) {
+#define BES_AXPY_CASE(n) \
+  case n: axpy_reduce_kernel<T, n, false><<<G, 256, 0, s>>>(w, V, ldv, h, N, partials); break;
+      BES_NV_CASES(BES_AXPY_CASE)
+#undef BES_AXPY_CASE
+      default: break;
+    }
   }
 }
 

@@ -56,9 +56,9 @@ class Options(ctypes.Structure):
         ("linear_solver", ctypes.c_int32), ("linear_solver_max_iter", ctypes.c_int32),
         ("gmres_restart", ctypes.c_int32), ("linear_solver_tol", ctypes.c_double),
         ("jacobian_repeat", ctypes.c_int32), ("precision", ctypes.c_int32),
-        ("cfl_ramp_steps", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("cfl_ramp_steps", ctypes.c_int32), ("freestream_ramp", ctypes.c_int32),
         ("cfl_ramp_start", ctypes.c_double), ("cfl_ramp_end", ctypes.c_double),
-        ("reserved", ctypes.c_double * 4),
+        ("freestream_ramp_start_frac", ctypes.c_double), ("reserved", ctypes.c_double * 3),
     ]
 
 

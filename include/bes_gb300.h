@@ -74,9 +74,11 @@ typedef struct {
   int32_t jacobian_repeat;        /* times each Jacobian block is added (Q9, default 5) */
   int32_t precision;              /* PRECISION (additive): 0 FP64, 1 FP32 linear solve */
   int32_t cfl_ramp_steps;         /* CFL_RAMP (additive): steps of a geometric CFL ramp, 0 off */
-  int32_t reserved0;
+  int32_t freestream_ramp;        /* FREESTREAM_RAMP: steps over which the freestream velocity
+                                     ramps up (src/Config.cpp:688-706), 0 off */
   double cfl_ramp_start, cfl_ramp_end;
-  double reserved[4];
+  double freestream_ramp_start_frac;  /* FREESTREAM_RAMP_START_FRAC (default 0.5) */
+  double reserved[3];
 } bes_options;
 
 typedef struct bes_ctx bes_ctx;

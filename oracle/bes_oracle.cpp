@@ -206,20 +206,32 @@ struct Oracle {
   std::vector<int64_t> blk_own_own, blk_own_nb, blk_nb_own, blk_nb_nb;  // per face block ids
   std::vector<double> JL, JR, rhs, dW;
   std::vector<int64_t> ilu_order;
+  std::vector<int64_t> ilu_domain;  // optional subdomain per cell (block Jacobi over them)
   double cfl_actual = 0;
   double maxres[5] = {0, 0, 0, 0, 0}, maxres_old[5] = {0, 0, 0, 0, 0};
   int step_count = 0;
+  int64_t solver_step = 0;  // iteration / pseudo-time step index (freestream ramp)
   int last_lin_iters = 0;
   double last_lin_err = 0;
   char err[256] = {0};
 };
 
-static void init_state(Oracle& O) {
-  // Config::initializePostMesh freestream primitives (src/Config.cpp:480-488)
+// Config::getFreestreamPrimitiveVariables (src/Config.cpp:688-706)
+static void set_freestream_for_step(Oracle& O, int64_t t) {
   O.Pinf[0] = 1.0;
   for (int d = 0; d < 3; ++d) O.Pinf[1 + d] = O.o.mach[d];
   O.Pinf[4] = 1.0 / O.o.gamma;
   O.Pinf[5] = 1.0 / (O.o.gamma * O.o.gas_constant);
+  if (O.o.fs_ramp > 0 && t < O.o.fs_ramp)
+    for (int d = 0; d < 3; ++d)
+      O.Pinf[1 + d] = O.o.mach[d] * (O.o.fs_frac + static_cast<double>(t) /
+                                                       static_cast<double>(O.o.fs_ramp) *
+                                                       (1 - O.o.fs_frac));
+}
+
+static void init_state(Oracle& O) {
+  // Config::initializePostMesh freestream primitives (src/Config.cpp:480-488)
+  set_freestream_for_step(O, 0);
   double U[5];
   O.g.conserved(O.Pinf, U);  // setUniversalInitialCondition (SolverExplicit.cpp:233-257)
   O.Un.assign(O.M.nc * 5, 0);
@@ -410,6 +422,7 @@ static void norms(const Mesh& M, const std::vector<double>& R, double* out10) {
 
 // SolverExplicit::timeStep_ (src/SolverExplicit.cpp:259-393)
 static void explicit_iteration(Oracle& O, double* norms10) {
+  set_freestream_for_step(O, O.solver_step++);
   compute_dt(O, O.Un.data(), O.o.cfl);
   const Mesh& M = O.M;
   for (int k = 0; k < O.o.n_stage; ++k) {
@@ -546,6 +559,7 @@ static void implicit_step(Oracle& O, double* hist) {
     O.maxres[v] = 0;
   }
   const double cfl = implicit_cfl_for_step(O);
+  set_freestream_for_step(O, O.solver_step++);
   const double* U = O.Un.data();
   compute_dt(O, U, cfl);
   compute_gradient(O, U);
@@ -602,6 +616,7 @@ static void implicit_step(Oracle& O, double* hist) {
     }
   }
   besla::Preconditioner P;
+  P.dom = O.ilu_domain;
   if (O.o.lin_precond == 1)
     P.setup_ilu0(O.A, O.ilu_order);
   else
@@ -668,6 +683,8 @@ struct bor_options {
   double venkat_k, harten, gas_constant, gamma;
   double mach[3];
   double lin_tol, ramp_cfl0, ramp_cfl1;
+  int32_t fs_ramp, pad2;
+  double fs_frac;
 };
 
 void* bor_create(const double* nodes, int64_t nv, const int64_t* tets, int64_t nc,
@@ -698,6 +715,8 @@ void* bor_create(const double* nodes, int64_t nv, const int64_t* tets, int64_t n
   o.lin_tol = op->lin_tol;
   o.ramp_cfl0 = op->ramp_cfl0;
   o.ramp_cfl1 = op->ramp_cfl1;
+  o.fs_ramp = op->fs_ramp;
+  o.fs_frac = op->fs_frac;
   O->threads = op->threads > 0 ? op->threads : 1;
   O->g.init(o.gas_constant, o.gamma);
   if (!bor::build_mesh(nodes, tets, nc, btris, btags, nb, o.muscl_exact, O->M, O->err)) {
@@ -765,6 +784,7 @@ void bor_operators(void* h, double cfl, double* dt, double* G, double* phi, doub
   bor::Oracle* O = static_cast<bor::Oracle*>(h);
   const bor::Mesh& M = O->M;
   const double* U = O->Un.data();
+  bor::set_freestream_for_step(*O, O->solver_step);  // the freestream of the next step
   bor::compute_dt(*O, U, cfl);
   bor::compute_gradient(*O, U);
   bor::compute_limiter(*O, U);
@@ -787,6 +807,14 @@ void bor_operators(void* h, double cfl, double* dt, double* G, double* phi, doub
 void bor_explicit_run(void* h, int64_t n, double* hist) {
   bor::Oracle* O = static_cast<bor::Oracle*>(h);
   for (int64_t i = 0; i < n; ++i) bor::explicit_iteration(*O, hist ? &hist[i * 10] : nullptr);
+}
+
+void bor_set_ilu_domain(void* h, const int64_t* dom) {
+  bor::Oracle* O = static_cast<bor::Oracle*>(h);
+  if (dom)
+    O->ilu_domain.assign(dom, dom + O->M.nc);
+  else
+    O->ilu_domain.clear();
 }
 
 void bor_set_ilu_order(void* h, const int64_t* order) {
@@ -832,6 +860,7 @@ int64_t bor_implicit_assemble(void* h, double cfl, double* rhs, double* vals, in
   bor::implicit_step(*O, loc);
   O->o.lin_maxiter = lp;
   O->Un = U0;
+  --O->solver_step;
   std::memcpy(O->maxres, mr, sizeof(mr));
   std::memcpy(O->maxres_old, mro, sizeof(mro));
   O->o.ramp_steps = ramp;

@@ -323,6 +323,8 @@ struct Options {
   // CFL ramp (new, additive): if ramp_steps > 0, CFL_k = cfl0 * (cfl1/cfl0)^(k/(ramp_steps-1))
   int ramp_steps = 0;
   double ramp_cfl0 = 0.0, ramp_cfl1 = 0.0;
+  int fs_ramp = 0;          // FREESTREAM_RAMP
+  double fs_frac = 0.5;     // FREESTREAM_RAMP_START_FRAC
 };
 
 }  // namespace bor

@@ -107,6 +107,10 @@ struct Preconditioner {
   // IKJ block ILU(0) in the given order: for row i (in order), for each block (i,j) with
   // pos[j] < pos[i] taken in increasing pos[j]: L_ij = A_ij * inv(U_jj); then for every
   // block (i,k) of row i with pos[k] > pos[j] that also exists in row j: A_ik -= L_ij*U_jk.
+  std::vector<int64_t> dom;       // optional subdomain id per cell: couplings between
+                                  // subdomains are dropped (block Jacobi over subdomains)
+  bool same(int64_t a, int64_t b) const { return dom.empty() || dom[a] == dom[b]; }
+
   void setup_ilu0(const BlockCsr& A, const std::vector<int64_t>& ord) {
     kind = 1;
     n = A.n;
@@ -123,7 +127,7 @@ struct Preconditioner {
       // lower blocks sorted by factorisation position
       std::vector<int64_t> lower;
       for (int64_t k = b0; k < b1; ++k)
-        if (pos[lu.col[k]] < p) lower.push_back(k);
+        if (pos[lu.col[k]] < p && same(i, lu.col[k])) lower.push_back(k);
       for (size_t a = 1; a < lower.size(); ++a)
         for (size_t b = a; b > 0 && pos[lu.col[lower[b]]] < pos[lu.col[lower[b - 1]]]; --b)
           std::swap(lower[b], lower[b - 1]);
@@ -134,7 +138,7 @@ struct Preconditioner {
         std::memcpy(&lu.val[kl * NB2], lij, sizeof(lij));
         for (int64_t kj = lu.row[j]; kj < lu.row[j + 1]; ++kj) {
           const int64_t c = lu.col[kj];
-          if (pos[c] <= pos[j]) continue;  // only U part of row j
+          if (pos[c] <= pos[j] || !same(j, c)) continue;  // only U part of row j
           const int64_t ki = lookup[c];
           if (ki < 0) continue;  // outside the pattern of row i: dropped (zero fill)
           double t[NB2];
@@ -161,7 +165,7 @@ struct Preconditioner {
       for (int q = 0; q < NB; ++q) acc[q] = r[i * NB + q];
       for (int64_t k = lu.row[i]; k < lu.row[i + 1]; ++k) {
         const int64_t j = lu.col[k];
-        if (pos[j] >= p) continue;
+        if (pos[j] >= p || !same(i, j)) continue;
         double t[NB];
         mat5_vec(&lu.val[k * NB2], &y[j * NB], t);
         for (int q = 0; q < NB; ++q) acc[q] -= t[q];
@@ -175,7 +179,7 @@ struct Preconditioner {
       for (int q = 0; q < NB; ++q) acc[q] = y[i * NB + q];
       for (int64_t k = lu.row[i]; k < lu.row[i + 1]; ++k) {
         const int64_t j = lu.col[k];
-        if (pos[j] <= p) continue;
+        if (pos[j] <= p || !same(i, j)) continue;
         double t[NB];
         mat5_vec(&lu.val[k * NB2], &z[j * NB], t);
         for (int q = 0; q < NB; ++q) acc[q] -= t[q];

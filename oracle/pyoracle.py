@@ -46,6 +46,7 @@ class _Opts(ctypes.Structure):
         ("gas_constant", ctypes.c_double), ("gamma", ctypes.c_double),
         ("mach", ctypes.c_double * 3), ("lin_tol", ctypes.c_double),
         ("ramp_cfl0", ctypes.c_double), ("ramp_cfl1", ctypes.c_double),
+        ("fs_ramp", ctypes.c_int32), ("pad2", ctypes.c_int32), ("fs_frac", ctypes.c_double),
     ]
 
 
@@ -54,7 +55,7 @@ DEFAULTS = dict(solver=0, local_dt=1, n_stage=4, muscl_exact=0, jacobian_repeat=
                 cfl=0.8, cfl_max=0.0, cfl_exp=(1.0, 1.0),
                 alpha=(0.0833, 0.2069, 0.4265, 1.0), venkat_k=5.0, harten=0.05,
                 gas_constant=287.0, gamma=1.4, mach=(0.5, 0.0, 0.0), lin_tol=1e-7,
-                ramp_cfl0=0.0, ramp_cfl1=0.0)
+                ramp_cfl0=0.0, ramp_cfl1=0.0, fs_ramp=0, fs_frac=0.5)
 
 _lib = None
 
@@ -80,6 +81,7 @@ def lib():
         L.bor_explicit_run.argtypes = [P, ctypes.c_int64, D]
         L.bor_implicit_run.argtypes = [P, ctypes.c_int64, D]
         L.bor_set_ilu_order.argtypes = [P, I64]
+        L.bor_set_ilu_domain.argtypes = [P, I64]
         L.bor_implicit_assemble.restype = ctypes.c_int64
         L.bor_implicit_assemble.argtypes = [P, ctypes.c_double, D, D, I64, I64]
         L.bor_flux_batch.argtypes = [P, ctypes.c_int32, ctypes.c_int64, D, D, D, D, D, D]
@@ -101,10 +103,10 @@ def make_opts(**kw) -> _Opts:
     cfg.update(kw)
     o = _Opts()
     for k in ("solver", "local_dt", "n_stage", "muscl_exact", "jacobian_repeat", "lin_precond",
-              "lin_restart", "lin_maxiter", "ramp_steps", "threads"):
+              "lin_restart", "lin_maxiter", "ramp_steps", "threads", "fs_ramp"):
         setattr(o, k, int(cfg[k]))
     for k in ("cfl", "cfl_max", "venkat_k", "harten", "gas_constant", "gamma", "lin_tol",
-              "ramp_cfl0", "ramp_cfl1"):
+              "ramp_cfl0", "ramp_cfl1", "fs_frac"):
         setattr(o, k, float(cfg[k]))
     o.cfl_exp0, o.cfl_exp1 = (float(x) for x in cfg["cfl_exp"])
     al = list(cfg["alpha"]) + [0.0] * (8 - len(cfg["alpha"]))
@@ -184,6 +186,12 @@ class Oracle:
     def set_ilu_order(self, order):
         order = np.ascontiguousarray(order, dtype=np.int64)
         lib().bor_set_ilu_order(self.h, _i(order))
+
+    def set_ilu_domain(self, dom):
+        """Subdomain id per cell (reference numbering); couplings between subdomains are left
+        out of the block-ILU(0) preconditioner.  None restores the global factorisation."""
+        d = None if dom is None else np.ascontiguousarray(dom, dtype=np.int64)
+        lib().bor_set_ilu_domain(self.h, _i(d))
 
     def implicit_run(self, n: int) -> np.ndarray:
         h = np.zeros((n, 19))

@@ -15,7 +15,8 @@ MESHES = {
 }
 
 CASES = ["explicit_bump_local", "explicit_bump_global", "explicit_gauss_pitch",
-         "explicit_bump_supersonic", "implicit_bump_jacobi", "implicit_bump_ilu0"]
+         "explicit_bump_supersonic", "explicit_bump_ramp", "implicit_bump_jacobi",
+         "implicit_bump_ilu0"]
 
 
 def load(name):
@@ -32,7 +33,8 @@ def mesh_of(info):
 def oracle_kwargs(info):
     m = info["meta"]
     kw = dict(solver=0 if m["solver"] == "EXPLICIT" else 1,
-              local_dt=1 if m["local"] == "YES" else 0, cfl=m["cfl"], mach=tuple(m["mach"]))
+              local_dt=1 if m["local"] == "YES" else 0, cfl=m["cfl"], mach=tuple(m["mach"]),
+              fs_ramp=m.get("fs_ramp", 0), fs_frac=m.get("fs_frac", 0.5))
     if m["solver"] == "IMPLICIT":
         kw.update(cfl_max=m["cfl_max"], cfl_exp=(1.0, 1.0),
                   lin_precond=1 if m["smoother"] == "ILU0" else 0, lin_tol=m["lin_tol"],

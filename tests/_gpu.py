@@ -14,7 +14,9 @@ def context(mesh, **opts):
 def explicit_opts(info):
     m = info["meta"]
     return dict(solver_type=0, local_time_step=1 if m["local"] == "YES" else 0,
-                courant_num=float(m["cfl"]), freestream_mach=tuple(m["mach"]))
+                courant_num=float(m["cfl"]), freestream_mach=tuple(m["mach"]),
+                freestream_ramp=int(m.get("fs_ramp", 0)),
+                freestream_ramp_start_frac=float(m.get("fs_frac", 0.5)))
 
 
 def rel_err(a, b):
@@ -23,7 +25,7 @@ def rel_err(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
-def hist_rel_err(h, ref, floor=1e-9):
+def hist_rel_err(h, ref, floor=1e-4):
     """Largest relative difference of two norm histories ([steps, k]).  Each entry is compared
     relative to itself, but never to less than `floor` times the largest norm of the same
     group of five (L2 or max) in that step: a variable whose residual is pure rounding noise

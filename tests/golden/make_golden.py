@@ -42,6 +42,10 @@ CASES = {
                                  dict(solver="EXPLICIT", local="YES", cfl=0.8,
                                       mach=(1.6, 0, 0)),
                                  20, "explicit", True),
+    "explicit_bump_ramp": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+                           dict(solver="EXPLICIT", local="YES", cfl=0.8, mach=(0.7, 0, 0),
+                                fs_ramp=8, fs_frac=0.3),
+                           15, "explicit", False),
     "implicit_bump_jacobi": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
                              dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
                                   mach=(0.84, 0, 0), smoother="DAMPED_JACOBI", lin_tol=1e-2,
@@ -69,6 +73,9 @@ def besi_text(mesh_path: str, out_dir: str, o: dict, steps: int) -> str:
         "SAVE_INTERVAL = 100000",
         "FREESTREAM_MACH = " + ", ".join(repr(float(x)) for x in o["mach"]),
     ]
+    if o.get("fs_ramp"):
+        lines += [f"FREESTREAM_RAMP = {o['fs_ramp']}",
+                  f"FREESTREAM_RAMP_START_FRAC = {o['fs_frac']!r}"]
     if o["solver"] == "IMPLICIT":
         lines += [
             f"ADAPTIVE_COURANT_NUM_MAX = {o['cfl_max']!r}",

@@ -68,6 +68,9 @@ def test_implicit_history_matches_oracle(case):
     O = pyoracle.Oracle(mesh, **G.oracle_kwargs(info))
     O.set_ilu_order(ctx.ilu_order())
     ho = O.implicit_run(n)
+    per_step = [hist_rel_err(h[k:k + 1, :12], ho[k:k + 1, :12]) for k in range(n)]
+    print("per-step rel err", per_step)
+    print("linear iterations gpu", h[:, 12], "oracle", ho[:, 12])
     assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
     assert hist_rel_err(h[:, 14:19], ho[:, 14:19]) <= 1e-9  # unscaled residual L2
     assert np.array_equal(h[:, 12], ho[:, 12])  # linear iterations
