@@ -75,16 +75,30 @@ def test_renumbering_is_a_permutation_and_groups_faces():
     assert np.all(np.diff(kinds) >= 0)
 
 
-def test_rcm_reduces_bandwidth():
+def _pages_per_warp(new2ref, own, nb):
+    """Average number of distinct 32-cell pages the face neighbours of a warp of 32
+    consecutive cells fall into (the gather footprint of a cell sweep)."""
+    n = len(new2ref)
+    inv = np.empty_like(new2ref)
+    inv[new2ref] = np.arange(n)
+    mask = nb >= 0
+    a, b = inv[own[mask]], inv[nb[mask]]
+    cells = np.concatenate([a, b])
+    nbrs = np.concatenate([b, a])
+    key = (cells // 32) * (n // 32 + 1) + nbrs // 32
+    uniq = np.unique(key)
+    return len(uniq) / (n / 32)
+
+
+def test_renumbering_keeps_neighbours_close():
+    """Cells are numbered colour by colour, each colour in reverse Cuthill-McKee order: the
+    neighbours of a warp of consecutive cells stay in a few pages, unlike a random order."""
     m = meshgen.bump_channel(30, 10, 8, 0.04)
     g = lib.host_geometry(m)
-    inv = np.empty_like(g["cell_new2ref"])
-    inv[g["cell_new2ref"]] = np.arange(len(inv))
     own, nb = g["face_owner"], g["face_neigh"]
-    mask = nb >= 0
-    bw_new = np.abs(inv[own[mask]] - inv[nb[mask]]).max()
-    bw_old = np.abs(own[mask] - nb[mask]).max()
-    assert bw_new <= bw_old
+    new = _pages_per_warp(g["cell_new2ref"], own, nb)
+    rnd = _pages_per_warp(np.random.default_rng(0).permutation(len(g["cell_new2ref"])), own, nb)
+    assert new < 0.25 * rnd
 
 
 def test_mesh_errors_are_reported():
