@@ -198,25 +198,29 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       precond_apply(S, S.Vk(j), S.Z);
       spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.Z, nullptr, S.W);
       ++S.c->launches;
+      // classical Gram-Schmidt, two passes; coefficients stay on the device
+      // (dev[0..31] first pass, dev[32..63] second pass, dev[64] |w|^2) and reach the host
+      // once per iteration
+      double* dev = c->imp.red_out;
       launch_dots<T>(j + 1, G, S.s, S.V, S.N, S.W, S.N, red);
-      ++S.c->launches;
-      if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h.data()))) return rc;
-      IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h.data(), (j + 1) * sizeof(double),
-                                 cudaMemcpyHostToDevice, S.s));
-      launch_axpy<T>(j + 1, true, G, S.s, S.W, S.V, S.N, c->imp.coef, S.N, red);
-      ++S.c->launches;
-      if ((rc = reduce_to_host(c, j + 1, G, j + 1, 0, h2.data()))) return rc;
-      IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, h2.data(), (j + 1) * sizeof(double),
-                                 cudaMemcpyHostToDevice, S.s));
-      launch_axpy<T>(j + 1, false, G, S.s, S.W, S.V, S.N, c->imp.coef, S.N, red);
-      ++S.c->launches;
-      double hn2;
-      if ((rc = reduce_to_host(c, 1, G, 1, 0, &hn2))) return rc;
+      reduce_rows_kernel<<<j + 1, 256, 0, S.s>>>(red, G, j + 1, 0, dev);
+      launch_axpy<T>(j + 1, true, G, S.s, S.W, S.V, S.N, dev, S.N, red);
+      reduce_rows_kernel<<<j + 1, 256, 0, S.s>>>(red, G, j + 1, 0, dev + 32);
+      launch_axpy<T>(j + 1, false, G, S.s, S.W, S.V, S.N, dev + 32, S.N, red);
+      reduce_rows_kernel<<<1, 256, 0, S.s>>>(red, G, 1, 0, dev + 64);
+      normalize_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(j + 1), S.W, dev + 64, S.N);
+      S.c->launches += 7;
+      double hbuf[65];
+      IMP_TRY(c, cudaMemcpyAsync(hbuf, dev, sizeof(hbuf), cudaMemcpyDeviceToHost, S.s));
+      IMP_TRY(c, cudaStreamSynchronize(S.s));
+      for (int i = 0; i <= j; ++i) {
+        h[i] = hbuf[i];
+        h2[i] = hbuf[32 + i];
+      }
+      const double hn2 = hbuf[64];
       for (int i = 0; i <= j; ++i) H[i * mr + j] = h[i] + h2[i];
       const double hn = std::sqrt(hn2);
       H[(j + 1) * mr + j] = hn;
-      if (hn != 0.0) scale_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(j + 1), S.W, 1.0 / hn, S.N);
-      ++S.c->launches;
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * H[i * mr + j] + sn[i] * H[(i + 1) * mr + j];
         H[(i + 1) * mr + j] = -sn[i] * H[i * mr + j] + cs[i] * H[(i + 1) * mr + j];
@@ -345,7 +349,7 @@ int implicit_allocate(bes_ctx* c) {
   rc |= imp_malloc(c, &I.X, N * I.tsize);
   rc |= imp_malloc(c, (void**)&I.rhs, N * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.red, 64 * (size_t)std::max<int64_t>(kRedBlocks, nblk(nc, 128)) * sizeof(double));
-  rc |= imp_malloc(c, (void**)&I.red_out, 64 * sizeof(double));
+  rc |= imp_malloc(c, (void**)&I.red_out, 128 * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.coef, 64 * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.m_own, nf);
   rc |= imp_malloc(c, (void**)&I.m_nb, nf);

@@ -440,9 +440,18 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restric
     y[(int64_t)r * nc + i] = b ? b[(int64_t)r * nc + i] - acc[r] : acc[r];
 }
 
-// Block reduction of NV per-thread double accumulators; partials[k*gridDim + blk].
-template <int NV>
-__device__ __forceinline__ void block_reduce_store(double (&acc)[NV], double* partials) {
+// Per-thread accumulation type of the vector kernels: the FP32 system accumulates each
+// thread's few elements in FP32 (the FP64 pipe is ~60x slower on this GPU) and reduces
+// across threads and blocks in FP64; the FP64 system stays FP64 throughout.
+template <class T> struct AccType { typedef double type; };
+template <> struct AccType<float> { typedef float type; };
+
+// Block reduction of NV per-thread accumulators; partials[k*gridDim + blk] (FP64).
+template <int NV, class A>
+__device__ __forceinline__ void block_reduce_store(A (&acc_in)[NV], double* partials) {
+  double acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) acc[k] = (double)acc_in[k];
   __shared__ double sh[NV][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -465,16 +474,17 @@ template <class T, int NV>
 __global__ void __launch_bounds__(256) dots_kernel(const T* __restrict__ V, int64_t ldv,
                                                    const T* __restrict__ w, int64_t N,
                                                    double* __restrict__ partials) {
-  double acc[NV];
+  typedef typename AccType<T>::type A;
+  A acc[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+  for (int k = 0; k < NV; ++k) acc[k] = A(0);
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    const double wv = (double)w[idx];
+    const A wv = (A)w[idx];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] += (double)V[(int64_t)k * ldv + idx] * wv;
+    for (int k = 0; k < NV; ++k) acc[k] += (A)V[(int64_t)k * ldv + idx] * wv;
   }
-  block_reduce_store<NV>(acc, partials);
+  block_reduce_store<NV, A>(acc, partials);
 }
 
 // w -= sum_k h_k V_k (k < NV) in one pass; then DOTS: partial V_k . w_new, or else partial
@@ -483,32 +493,33 @@ template <class T, int NV, bool DOTS>
 __global__ void __launch_bounds__(256) axpy_reduce_kernel(T* __restrict__ w, const T* __restrict__ V,
                                                           int64_t ldv, const double* __restrict__ h,
                                                           int64_t N, double* __restrict__ partials) {
-  double hs[NV];
+  typedef typename AccType<T>::type A;
+  A hs[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) hs[k] = h[k];
+  for (int k = 0; k < NV; ++k) hs[k] = (A)h[k];
   constexpr int NA = DOTS ? NV : 1;
-  double acc[NA];
+  A acc[NA];
 #pragma unroll
-  for (int k = 0; k < NA; ++k) acc[k] = 0.0;
+  for (int k = 0; k < NA; ++k) acc[k] = A(0);
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x) {
     T v[NV];
-    double x = (double)w[idx];
+    A x = (A)w[idx];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       v[k] = V[(int64_t)k * ldv + idx];
-      x -= hs[k] * (double)v[k];
+      x -= hs[k] * (A)v[k];
     }
     const T xt = (T)x;
     w[idx] = xt;
     if (DOTS) {
 #pragma unroll
-      for (int k = 0; k < NA; ++k) acc[k] += (double)v[k] * (double)xt;
+      for (int k = 0; k < NA; ++k) acc[k] += (A)v[k] * (A)xt;
     } else {
-      acc[0] += (double)xt * (double)xt;
+      acc[0] += (A)xt * (A)xt;
     }
   }
-  block_reduce_store<NA>(acc, partials);
+  block_reduce_store<NA, A>(acc, partials);
 }
 
 // Launch helpers dispatching the vector count to a compile-time constant (1..32).
@@ -553,9 +564,26 @@ void launch_axpy(int nvec, bool dots, int G, cudaStream_t s, T* w, const T* V, i
 template <class T>
 __global__ void __launch_bounds__(256) scale_kernel(T* __restrict__ out, const T* __restrict__ in,
                                                     double s, int64_t N) {
+  typedef typename AccType<T>::type A;
+  const A sa = (A)s;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x)
-    out[idx] = (T)((double)in[idx] * s);
+    out[idx] = (T)((A)in[idx] * sa);
+}
+
+// out = in / sqrt(*norm2) (the new Arnoldi vector), left untouched when the norm is zero
+template <class T>
+__global__ void __launch_bounds__(256) normalize_kernel(T* __restrict__ out,
+                                                        const T* __restrict__ in,
+                                                        const double* __restrict__ norm2,
+                                                        int64_t N) {
+  typedef typename AccType<T>::type A;
+  const double n2 = *norm2;
+  if (!(n2 > 0.0)) return;
+  const A sa = (A)(1.0 / sqrt(n2));
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    out[idx] = (T)((A)in[idx] * sa);
 }
 
 // out = sum_k y_k V_k
@@ -563,13 +591,14 @@ template <class T>
 __global__ void __launch_bounds__(256) lincomb_kernel(T* __restrict__ out, const T* __restrict__ V,
                                                       int64_t ldv, int nvec,
                                                       const double* __restrict__ y, int64_t N) {
-  __shared__ double ys[64];
-  for (int k = threadIdx.x; k < nvec; k += blockDim.x) ys[k] = y[k];
+  typedef typename AccType<T>::type A;
+  __shared__ A ys[64];
+  for (int k = threadIdx.x; k < nvec; k += blockDim.x) ys[k] = (A)y[k];
   __syncthreads();
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    double x = 0.0;
-    for (int k = 0; k < nvec; ++k) x += ys[k] * (double)V[(int64_t)k * ldv + idx];
+    A x = A(0);
+    for (int k = 0; k < nvec; ++k) x += ys[k] * (A)V[(int64_t)k * ldv + idx];
     out[idx] = (T)x;
   }
 }
@@ -588,11 +617,12 @@ template <class T>
 __global__ void __launch_bounds__(256) norm2_kernel(const T* __restrict__ x, int64_t N,
                                                     double* __restrict__ partials) {
   __shared__ double sh[8];
-  double s = 0.0;
+  typedef typename AccType<T>::type A;
+  A sa = A(0);
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x)
-    s += (double)x[idx] * (double)x[idx];
-  s = warp_sum(s);
+    sa += (A)x[idx] * (A)x[idx];
+  double s = warp_sum((double)sa);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x < 32) {
