@@ -163,12 +163,14 @@ extern "C" int bes_options_from_besi(const char* path, bes_options* o, char* mes
         if (!num(d, o->freestream_mach[d])) return bad("FREESTREAM_MACH needs three numbers");
     } else if (key == "LINEAR_SOLVER") {
       // FGMRES/GMRES/LGMRES/BICGSTAB (the reference's AMGCL solvers) all map to GMRES(m);
-      // BLOCK_JACOBI_GMRES / BLOCK_ILU0_GMRES select the preconditioner explicitly.
+      // BLOCK_JACOBI_GMRES / BLOCK_ILU0_GMRES (colour order) / BLOCK_ILU0_RCM_GMRES (reverse
+      // Cuthill-McKee order, level scheduled) select the preconditioner explicitly.
       const int w = word({"FGMRES", "GMRES", "LGMRES", "BICGSTAB", "BLOCK_JACOBI_GMRES",
-                          "BLOCK_ILU0_GMRES"});
+                          "BLOCK_ILU0_GMRES", "BLOCK_ILU0_RCM_GMRES"});
       if (w < 0) return bad("Linear solver option not supported");
       if (w == 4) o->linear_solver = 0;
       if (w == 5) o->linear_solver = 1;
+      if (w == 6) o->linear_solver = 2;
     } else if (key == "AMG_PRECOND_COARSENER") {
       if (word({"AGGREGATION", "SMOOTHED_AGGREGATION", "SMOOTHED_AGGREGATION_EMIN",
                 "RUGE_STUBEN"}) < 0)

@@ -268,6 +268,8 @@ void bes_destroy(bes_ctx* ctx) {
   for (int k = 0; k < 8; ++k)
     for (int q = 0; q < 6; ++q)
       if (ctx->kev[k][q]) cudaEventDestroy(ctx->kev[k][q]);
+  if (ctx->imp.factor_graph) cudaGraphExecDestroy(ctx->imp.factor_graph);
+  if (ctx->imp.apply_graph) cudaGraphExecDestroy(ctx->imp.apply_graph);
   for (void* p : ctx->allocations) cudaFree(p);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;

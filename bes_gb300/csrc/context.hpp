@@ -75,8 +75,10 @@ struct ImplicitBuffers {
   double* coef = nullptr;      // small coefficient vectors [64]
   int8_t* m_own = nullptr;     // per face local index in owner / neighbour
   int8_t* m_nb = nullptr;
-  int32_t* color_rows = nullptr;
-  int32_t* ilu_pos = nullptr;
+  int32_t* stage_rows = nullptr;  // block-ILU(0) rows grouped by stage
+  int32_t* ilu_pos = nullptr;     // factorisation position of each cell
+  cudaGraphExec_t factor_graph = nullptr;  // ILU factorisation, all stages
+  cudaGraphExec_t apply_graph = nullptr;   // ILU forward+backward sweep, in place on Z
   double cfl_actual = 0;
   double maxres[5] = {0, 0, 0, 0, 0};
   double maxres_old[5] = {0, 0, 0, 0, 0};

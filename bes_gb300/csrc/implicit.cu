@@ -81,23 +81,67 @@ int reduce_to_host(bes_ctx* c, int nrows, int nblocks, int nsum, int sqrt_sums, 
   return BES_OK;
 }
 
+inline bool uses_ilu(const bes_ctx* c) { return c->opt.linear_solver == 1 || c->opt.linear_solver == 2; }
+
+// Enqueue the block-ILU(0) sweeps in place on S.Z (stage by stage), for graph capture.
+template <class T>
+void enqueue_ilu_sweeps(const Sys<T>& S) {
+  bes_ctx* c = S.c;
+  const SoaMesh& M = c->soa;
+  for (int k = 0; k < M.n_stages; ++k) {
+    const int n = M.stage_off[k + 1] - M.stage_off[k];
+    ilu_lower_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
+                                                       n, c->imp.ilu_pos, S.LU, S.Z, S.Z);
+  }
+  for (int k = M.n_stages - 1; k >= 0; --k) {
+    const int n = M.stage_off[k + 1] - M.stage_off[k];
+    ilu_upper_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
+                                                       n, c->imp.ilu_pos, S.LU, S.Dinv, S.Z);
+  }
+}
+
+template <class T>
+void enqueue_ilu_factor(const Sys<T>& S) {
+  bes_ctx* c = S.c;
+  const SoaMesh& M = c->soa;
+  // the factors overwrite a copy: the Krylov products need the unfactored matrix
+  cudaMemcpyAsync(S.LU, S.A, (size_t)125 * S.nc * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
+  for (int k = 0; k < M.n_stages; ++k) {
+    const int n = M.stage_off[k + 1] - M.stage_off[k];
+    ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
+                                                        n, c->imp.ilu_pos, S.LU, S.Dinv);
+  }
+}
+
+// Capture the stage-by-stage ILU work once per context as CUDA graphs (hundreds of small
+// kernels under level scheduling).
+template <class T>
+int ensure_ilu_graphs(const Sys<T>& S) {
+  bes_ctx* c = S.c;
+  if (c->imp.apply_graph) return BES_OK;
+  cudaGraph_t g;
+  IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
+  enqueue_ilu_factor(S);
+  IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
+  IMP_TRY(c, cudaGraphInstantiate(&c->imp.factor_graph, g, 0));
+  cudaGraphDestroy(g);
+  IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
+  enqueue_ilu_sweeps(S);
+  IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
+  IMP_TRY(c, cudaGraphInstantiate(&c->imp.apply_graph, g, 0));
+  cudaGraphDestroy(g);
+  return BES_OK;
+}
+
+// out = M^{-1} in (out is always S.Z)
 template <class T>
 void precond_apply(const Sys<T>& S, const T* in, T* out) {
   bes_ctx* c = S.c;
-  const SoaMesh& M = c->soa;
-  if (c->opt.linear_solver == 1) {
-    for (int k = 0; k < M.n_colors; ++k) {
-      const int n = M.color_off[k + 1] - M.color_off[k];
-      ilu_lower_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
-                                                         n, c->imp.ilu_pos, S.LU, in, out);
-      ++S.c->launches;
-    }
-    for (int k = M.n_colors - 1; k >= 0; --k) {
-      const int n = M.color_off[k + 1] - M.color_off[k];
-      ilu_upper_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
-                                                         n, c->imp.ilu_pos, S.LU, S.Dinv, out);
-      ++S.c->launches;
-    }
+  if (uses_ilu(c)) {
+    if (in != out)
+      cudaMemcpyAsync(out, in, (size_t)S.N * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
+    cudaGraphLaunch(c->imp.apply_graph, S.s);
+    c->launches += 2 * c->soa.n_stages;
   } else {
     jacobi_apply_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, S.Dinv, in, out);
     ++S.c->launches;
@@ -105,18 +149,14 @@ void precond_apply(const Sys<T>& S, const T* in, T* out) {
 }
 
 template <class T>
-void precond_setup(const Sys<T>& S) {
+int precond_setup(const Sys<T>& S) {
   bes_ctx* c = S.c;
-  const SoaMesh& M = c->soa;
-  if (c->opt.linear_solver != 1) return;  // block Jacobi inverted during assembly
-  // the factors overwrite a copy: the Krylov products need the unfactored matrix
-  cudaMemcpyAsync(S.LU, S.A, (size_t)125 * S.nc * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
-  for (int k = 0; k < M.n_colors; ++k) {
-    const int n = M.color_off[k + 1] - M.color_off[k];
-    ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.color_rows + M.color_off[k],
-                                                        n, c->imp.ilu_pos, S.LU, S.Dinv);
-    ++S.c->launches;
-  }
+  if (!uses_ilu(c)) return BES_OK;  // block Jacobi inverted during assembly
+  int rc = ensure_ilu_graphs(S);
+  if (rc) return rc;
+  IMP_TRY(c, cudaGraphLaunch(c->imp.factor_graph, S.s));
+  c->launches += c->soa.n_stages;
+  return BES_OK;
 }
 
 // Residual, first-order Jacobians and the assembled system at the current state; returns the
@@ -143,7 +183,7 @@ int assemble(bes_ctx* c, double cfl, double* norms15) {
   const int nb = nblk(m.nc, 128);
   cell_assemble_kernel<T><<<nb, 128, 0, S.s>>>(m, c->FA, c->dt, c->dtmin, local,
                                                o.jacobian_repeat, S.Dc, S.A,
-                                               o.linear_solver == 1 ? nullptr : S.Dinv,
+                                               uses_ilu(c) ? nullptr : S.Dinv,
                                                c->imp.rhs, S.b, c->imp.red);
   ++S.c->launches;
   IMP_TRY(c, cudaGetLastError());
@@ -290,7 +330,8 @@ int implicit_step(bes_ctx* c, double* hist) {
   rc = check_nan_public(c);
   if (rc) return rc;
   Sys<T> S(c);
-  precond_setup(S);
+  rc = precond_setup(S);
+  if (rc) return rc;
   int iters = 0;
   double rel = 0.0;
   rc = gmres<T>(c, iters, rel);
@@ -340,7 +381,13 @@ int implicit_allocate(bes_ctx* c) {
   int rc = 0;
   rc |= imp_malloc(c, &I.A, 125 * nc * I.tsize);
   rc |= imp_malloc(c, &I.Dinv, 25 * nc * I.tsize);
-  if (o.linear_solver == 1) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
+  if (o.linear_solver < 0 || o.linear_solver > 2) {
+    c->last_error = "linear_solver must be 0 (block Jacobi), 1 (block ILU(0), colour order) or 2 "
+                    "(block ILU(0), RCM order, level scheduled)";
+    return BES_ERR_UNSUPPORTED;
+  }
+  if (o.linear_solver == 2) build_ilu_schedule(c->soa, true);
+  if (uses_ilu(c)) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
   rc |= imp_malloc(c, &I.b, N * I.tsize);
   rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * N * I.tsize);
@@ -353,13 +400,13 @@ int implicit_allocate(bes_ctx* c) {
   rc |= imp_malloc(c, (void**)&I.coef, 64 * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.m_own, nf);
   rc |= imp_malloc(c, (void**)&I.m_nb, nf);
-  rc |= imp_malloc(c, (void**)&I.color_rows, nc * sizeof(int32_t));
+  rc |= imp_malloc(c, (void**)&I.stage_rows, nc * sizeof(int32_t));
   rc |= imp_malloc(c, (void**)&I.ilu_pos, nc * sizeof(int32_t));
   if (rc) return BES_ERR_CUDA;
   IMP_TRY(c, cudaMemset(I.A, 0, 125 * nc * I.tsize));  // empty slots stay zero
   IMP_TRY(c, cudaMemcpy(I.m_own, M.f_m_own.data(), nf, cudaMemcpyHostToDevice));
   IMP_TRY(c, cudaMemcpy(I.m_nb, M.f_m_nb.data(), nf, cudaMemcpyHostToDevice));
-  IMP_TRY(c, cudaMemcpy(I.color_rows, M.color_rows.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice));
+  IMP_TRY(c, cudaMemcpy(I.stage_rows, M.stage_rows.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice));
   IMP_TRY(c, cudaMemcpy(I.ilu_pos, M.ilu_pos.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice));
   I.cfl_actual = o.courant_num;
   return BES_OK;
@@ -434,7 +481,7 @@ int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks,
 int bes_ilu_order(bes_ctx* ctx, int64_t* order) {
   if (!ctx || !order) return BES_ERR_INVALID;
   const SoaMesh& M = ctx->soa;
-  for (int64_t p = 0; p < M.nc; ++p) order[p] = M.cell_new2ref[M.color_rows[p]];
+  for (int64_t i = 0; i < M.nc; ++i) order[M.ilu_pos[i]] = M.cell_new2ref[i];
   return BES_OK;
 }
 

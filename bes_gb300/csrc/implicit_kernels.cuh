@@ -327,7 +327,7 @@ template <class T>
 __global__ void __launch_bounds__(128) ilu_lower_kernel(DevMesh m, const int32_t* __restrict__ rows,
                                                         int nrows, const int32_t* __restrict__ pos,
                                                         const T* __restrict__ A,
-                                                        const T* __restrict__ in, T* __restrict__ out) {
+                                                        const T* in, T* out) {  // may alias
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nrows) return;
   const int nc = m.nc;

@@ -361,8 +361,16 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
       while (used & (1u << k)) ++k;
       col[c] = k;
     }
+    std::vector<int64_t> rank_ref(nc);
+    for (int64_t p = 0; p < nc; ++p) rank_ref[S.cell_new2ref[p]] = p;
     std::stable_sort(S.cell_new2ref.begin(), S.cell_new2ref.end(),
                      [&](int64_t a, int64_t b) { return col[a] < col[b]; });
+    S.rcm_rank.resize(nc);
+    for (int64_t i = 0; i < nc; ++i) S.rcm_rank[i] = rank_ref[S.cell_new2ref[i]];
+  }
+  if (S.rcm_rank.empty()) {
+    S.rcm_rank.resize(nc);
+    std::iota(S.rcm_rank.begin(), S.rcm_rank.end(), 0);
   }
   S.cell_ref2new.assign(nc, -1);
   for (int64_t i = 0; i < nc; ++i) S.cell_ref2new[S.cell_new2ref[i]] = i;
@@ -520,19 +528,46 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
     ncol = std::max(ncol, col + 1);
   }
   S.n_colors = ncol;
-  S.color_off.assign(ncol + 1, 0);
-  for (int64_t i = 0; i < nc; ++i) S.color_off[S.cell_color[i] + 1]++;
-  for (int c = 0; c < ncol; ++c) S.color_off[c + 1] += S.color_off[c];
-  S.color_rows.assign(nc, 0);
+  build_ilu_schedule(S, false);
+}
+
+void build_ilu_schedule(SoaMesh& S, bool rcm_order) {
+  const int64_t nc = S.nc;
   S.ilu_pos.assign(nc, 0);
-  {
-    std::vector<int32_t> fill(S.color_off.begin(), S.color_off.end() - 1);
-    for (int64_t i = 0; i < nc; ++i) {
-      const int32_t p = fill[S.cell_color[i]]++;
-      S.color_rows[p] = (int32_t)i;
-      S.ilu_pos[i] = p;
+  std::vector<int32_t> stage(nc, 0);
+  int32_t nst = 0;
+  if (!rcm_order) {
+    // colour order: position = (colour, id); with colour-major numbering this is the identity
+    std::vector<int64_t> idx(nc);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int64_t a, int64_t b) { return S.cell_color[a] < S.cell_color[b]; });
+    for (int64_t p = 0; p < nc; ++p) S.ilu_pos[idx[p]] = (int32_t)p;
+    for (int64_t i = 0; i < nc; ++i) stage[i] = S.cell_color[i];
+    nst = S.n_colors;
+  } else {
+    // RCM order with level scheduling: level(i) = 1 + max level of its earlier neighbours
+    std::vector<int64_t> idx(nc);
+    for (int64_t i = 0; i < nc; ++i) idx[S.rcm_rank[i]] = i;
+    for (int64_t p = 0; p < nc; ++p) S.ilu_pos[idx[p]] = (int32_t)p;
+    for (int64_t p = 0; p < nc; ++p) {
+      const int64_t i = idx[p];
+      int32_t lv = 0;
+      for (int m = 0; m < 4; ++m) {
+        const int32_t a = S.adj[m * nc + i];
+        if (a >= 0 && S.ilu_pos[a] < p) lv = std::max(lv, stage[a] + 1);
+      }
+      stage[i] = lv;
+      nst = std::max(nst, lv + 1);
     }
   }
+  S.n_stages = nst;
+  S.stage_off.assign(nst + 1, 0);
+  for (int64_t i = 0; i < nc; ++i) S.stage_off[stage[i] + 1]++;
+  for (int k = 0; k < nst; ++k) S.stage_off[k + 1] += S.stage_off[k];
+  S.stage_rows.assign(nc, 0);
+  std::vector<int32_t> fill(S.stage_off.begin(), S.stage_off.end() - 1);
+  for (int64_t i = 0; i < nc; ++i) S.stage_rows[fill[stage[i]]++] = (int32_t)i;
 }
 
 }  // namespace bes

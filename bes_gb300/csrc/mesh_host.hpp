@@ -48,13 +48,23 @@ struct SoaMesh {
   // diagonal block first, then neighbours in local face order) with fixed-width rows.
   std::vector<int8_t> f_m_own, f_m_nb;   // local face index of each face in owner / neighbour
   std::vector<int32_t> cell_color;       // greedy colouring of the cell graph
-  std::vector<int32_t> color_rows;       // cells sorted by (colour, id): the ILU(0) order
-  std::vector<int32_t> color_off;        // [n_colors+1] offsets into color_rows
-  std::vector<int32_t> ilu_pos;          // cell -> position in color_rows
   int32_t n_colors = 0;
+  // Block-ILU(0) schedule: the factorisation order (ilu_pos: cell -> position) and its
+  // stages, groups of rows with no coupling to rows of the same or later stages, run one
+  // stage at a time.  Colour order: one stage per colour.  RCM order: one stage per level
+  // of the dependency graph (level scheduling).
+  std::vector<int32_t> ilu_pos;          // cell -> position in the factorisation order
+  std::vector<int32_t> stage_rows;       // cells grouped by stage
+  std::vector<int32_t> stage_off;        // [n_stages+1] offsets into stage_rows
+  int32_t n_stages = 0;
+  std::vector<int64_t> rcm_rank;         // reverse Cuthill-McKee position of each new cell
 };
 
 // Reverse Cuthill-McKee renumbering + face grouping + SoA packing.
 void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumber, SoaMesh& out);
+
+// Block-ILU(0) schedule: rcm_order = false -> colour order (stage = colour), true -> reverse
+// Cuthill-McKee order with level scheduling (stage = dependency level).
+void build_ilu_schedule(SoaMesh& S, bool rcm_order);
 
 }  // namespace bes

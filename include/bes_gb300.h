@@ -67,7 +67,8 @@ typedef struct {
   double specific_heat_ratio;     /* SPECIFIC_HEAT_RATIO (default 1.4) */
   double freestream_mach[3];      /* FREESTREAM_MACH */
   int32_t number_of_time_step;    /* NUMBER_OF_TIME_STEP */
-  int32_t linear_solver;          /* 0 block-Jacobi GMRES, 1 block-ILU(0) GMRES */
+  int32_t linear_solver;          /* 0 block-Jacobi GMRES, 1 block-ILU(0) GMRES (colour order),
+                                     2 block-ILU(0) GMRES (RCM order, level scheduled) */
   int32_t linear_solver_max_iter; /* LINEAR_SOLVER_MAX_ITER (default 1000) */
   int32_t gmres_restart;          /* GMRES_RESTART (additive, default 30) */
   double linear_solver_tol;       /* LINEAR_SOLVER_ABS_TOL: relative to |b| (default 1e-7) */
@@ -126,8 +127,9 @@ int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
 /* n implicit pseudo-time steps (SolverImplicit::timeStep_, src/SolverImplicit.cpp:293-345):
  * local/global dt at the step's CFL, second-order residual, first-order Jacobians assembled
  * into the 5x5-block system (each block added jacobian_repeat times, Q9), right-preconditioned
- * GMRES(gmres_restart) to linear_solver_tol relative with a block-Jacobi (linear_solver 0) or
- * colour-ordered block-ILU(0) (linear_solver 1) preconditioner, in FP64 (precision 0) or FP32
+ * GMRES(gmres_restart) to linear_solver_tol relative with a block-Jacobi (linear_solver 0),
+ * colour-ordered block-ILU(0) (1) or RCM-ordered level-scheduled block-ILU(0) (2)
+ * preconditioner, in FP64 (precision 0) or FP32
  * (precision 1, defect correction: residual, update and norms stay FP64), the update, and the
  * CFL control (adaptive as adaptCourantNum_, src/SolverImplicit.cpp:530-550, or the additive
  * geometric ramp).  history (may be NULL): [n][19] = L2[5] and max[5] of the Dt/V-scaled

@@ -113,3 +113,23 @@ def test_fp32_defect_correction_tracks_fp64(precond):
     # the residual histories follow each other
     assert np.max(np.abs(np.log(h32[:, :5] / h64[:, :5]))) <= 0.05
     assert np.all(h32[:, 12] >= 1)
+
+
+@pytest.mark.parametrize("linear_solver", [1, 2])
+def test_ilu_orders_match_oracle(linear_solver):
+    """Colour-ordered (1) and RCM-ordered level-scheduled (2) block ILU(0): the GPU's
+    factorisation order handed to the oracle gives the same iterates."""
+    mesh = meshgen.bump_channel(24, 8, 6, 0.08)
+    kw = dict(solver_type=1, local_time_step=1, courant_num=10.0, freestream_mach=(0.84, 0, 0),
+              linear_solver=linear_solver, linear_solver_tol=1e-2, linear_solver_max_iter=300,
+              gmres_restart=30, cfl_ramp_steps=8, cfl_ramp_start=10.0, cfl_ramp_end=500.0)
+    ctx = context(mesh, **kw)
+    h = ctx.implicit_steps(10)
+    O = pyoracle.Oracle(mesh, solver=1, local_dt=1, cfl=10.0, mach=(0.84, 0, 0), lin_precond=1,
+                        lin_tol=1e-2, lin_maxiter=300, lin_restart=30, ramp_steps=8,
+                        ramp_cfl0=10.0, ramp_cfl1=500.0)
+    O.set_ilu_order(ctx.ilu_order())
+    ho = O.implicit_run(10)
+    assert np.array_equal(h[:, 12], ho[:, 12])
+    assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
+    assert rel_err(ctx.get_state(), O.get_state()) <= 1e-9
