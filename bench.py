@@ -3,9 +3,12 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
                     [--workload explicit_bump_72k]
 
-A step is one pass of the hot path over the workload: one explicit multi-step iteration
-(4 stages of gradient + limiter + MUSCL, face fluxes and update) over every cell.  The metric
-is cell-updates/s = cells x steps / time.  Rank 0 prints one JSON line.
+Default workload: implicit backward Euler on the 200x60x30-hex bump channel (2.16M tets,
+Mach 0.84), block-ILU(0) GMRES(30) to 1e-2, CFL ramp 10 -> 1000 over 50 steps; the line's value
+is the FP32-system defect correction (FP64 residual and update), with the plain FP64 system
+measured on the same steps beside it.  A step is one pseudo-time step (explicit workloads: one
+4-stage iteration) over every cell; the metric is cell-updates/s = cells x steps / time.  Rank 0
+prints one JSON line.
 
 * value: device time from CUDA events on the library's stream around each step's graph
   launch, L2 flushed (256 MB write) before every timed step, summed over K steps; max over
@@ -50,7 +53,7 @@ WORKLOADS = {
     # first-order Roe Jacobian in 5x5 blocks, block-ILU(0) GMRES(30) to 1e-2 relative, CFL
     # ramped 10 -> 1000 over 50 steps; FP32 Jacobian/preconditioner/Krylov with FP64 residual
     # and update (defect correction), or everything FP64
-    "implicit_bump_2m_mixed": dict(kind="implicit", mesh=("bump", 200, 60, 30, 0.08),
+    "implicit_bump_2m": dict(kind="implicit", mesh=("bump", 200, 60, 30, 0.08),
                                    opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
                                              freestream_mach=(0.84, 0.0, 0.0), linear_solver=1,
                                              linear_solver_tol=1e-2, linear_solver_max_iter=300,
@@ -184,6 +187,20 @@ def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    if wl["kind"] == "implicit":
+        steps = max(1, min(args.steps, 3))
+        base = implicit_cpu_baseline(wl, steps=steps)
+        value = base["value"]
+        line = {"impl": "reference", "metric": METRIC, "metric_full": METRIC_FULL,
+                "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": steps,
+                "warmup": args.warmup, "ms_per_step": 72000 / value * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": args.workload},
+                "cpu_baseline": base,
+                "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
     mesh = make_mesh(wl["mesh"])
     steps = args.steps
     from oracle import pyoracle
@@ -217,40 +234,94 @@ def run_reference(args, wl):
     return 0
 
 
-def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
-    """One step = one implicit pseudo-time step (residual, Jacobian, assembly, linear solve,
-    update).  Device time from events on the library's stream around each step."""
+# Algorithmic bytes per cell of the implicit kernels with an FP32 system (4-byte values):
+#   preconditioner application (colour-ordered block ILU(0) forward + backward sweep): the
+#     four off-diagonal blocks once (4 x 100) + inverse diagonal block (100) + the vector read
+#     and written in both sweeps (4 x 20)                                          = 580
+#   matrix-vector product: five blocks (500) + x (20) + y (20)                       = 540
+# With an FP64 system the block and vector bytes double.
+BYTES_PRECOND = {1: 580.0, 0: 1160.0}
+BYTES_SPMV = {1: 540.0, 0: 1080.0}
+
+
+def implicit_leg(args, torch, ctx, steps, warmup, flush, with_e2e):
+    """warm-up, then `steps` timed implicit steps (events on the library stream around each
+    step, L2 flushed before each); returns timing, history and the kernel-category profile."""
     nc = ctx.n_cells
-    ctx.implicit_steps(args.warmup)
+    ctx.implicit_steps(warmup)
     ext = torch.cuda.ExternalStream(ctx.stream_handle)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     c0 = ctx.counters()
-    clocks = ClockSampler(local_rank)
+    ctx.profile(True)
     hist = []
-    if dist:
-        dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
-    for k in range(args.steps):
+    for k in range(steps):
         with torch.cuda.stream(ext):
             flush.fill_(float(k))
             starts[k].record(ext)
         hist.append(ctx.implicit_steps(1)[0])
         ends[k].record(ext)
     torch.cuda.synchronize()
-    clk = clocks.stop()
+    prof = ctx.profile(False)
     c1 = ctx.counters()
+    dev_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
+    out = dict(ms=dev_ms, hist=np.array(hist), prof=prof,
+               launches=c1["launches"] - c0["launches"])
+    if with_e2e:
+        U = ctx.get_state()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.set_state(U)
+            ctx.implicit_steps(1)
+            U = ctx.get_state()
+        out["e2e_s"] = time.perf_counter() - t0
+    return out
+
+
+def implicit_cpu_baseline(wl, steps: int = 2):
+    """The CPU restatement on a bounded sample: the same scheme and options on the 60x20x10
+    bump channel (72,000 cells), OpenMP on all host cores for the assembly."""
+    from bes_gb300 import meshgen
+    from oracle import pyoracle
+    o = wl["opts"]
+    threads = os.cpu_count() or 1
+    mesh = meshgen.bump_channel(60, 20, 10, 0.08)
+    O = pyoracle.Oracle(mesh, solver=1, local_dt=o["local_time_step"], cfl=o["courant_num"],
+                        mach=o["freestream_mach"], lin_precond=1, lin_tol=o["linear_solver_tol"],
+                        lin_maxiter=o["linear_solver_max_iter"], lin_restart=o["gmres_restart"],
+                        ramp_steps=o["cfl_ramp_steps"], ramp_cfl0=o["cfl_ramp_start"],
+                        ramp_cfl1=o["cfl_ramp_end"], threads=threads)
+    O.implicit_run(3)  # the same ramp position as the GPU's warm-up
+    t0 = time.perf_counter()
+    O.implicit_run(steps)
+    dt = time.perf_counter() - t0
+    return {"value": mesh.n_cells * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"implicit steps 4-{3 + steps} (block-ILU(0) GMRES, FP64) on the 60x20x10 "
+                      f"bump channel, {mesh.n_cells} cells (oracle/bes_oracle.cpp; OpenMP "
+                      f"{threads} threads in the assembly, serial linear solve)"}
+
+
+def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
+    """One step = one implicit pseudo-time step (residual, Jacobian, assembly, linear solve,
+    update).  value: the FP32-system defect correction (production form); the plain FP64
+    system is measured on the same steps for comparison."""
+    from bes_gb300 import lib
+    nc = ctx.n_cells
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(local_rank)
     if dist:
         dist.barrier()
-    dev_ms = float(sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
-    t_max = dev_ms
+    clocks.start()
+    mixed = implicit_leg(args, torch, ctx, args.steps, args.warmup, flush, with_e2e=False)
+    clk = clocks.stop()
+    t_max = mixed["ms"]
     if dist:
-        tt = torch.tensor([dev_ms], dtype=torch.float64)
+        tt = torch.tensor([t_max], dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max = float(tt.item())
     value = world * nc * args.steps / (t_max / 1e3)
+    # e2e through the C ABI with host buffers (state up, one step, state down)
     U = ctx.get_state()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -262,22 +333,47 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
         tt = torch.tensor([e2e_s], dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e2e_s = float(tt.item())
-    hist = np.array(hist)
-    lin = hist[:, 12]
+    # the plain FP64 system on the same steps
+    o64 = dict(wl["opts"])
+    o64["precision"] = 0
+    ctx64 = lib.Context(mesh, lib.default_options(**o64))
+    plain = implicit_leg(args, torch, ctx64, args.steps, args.warmup, flush, with_e2e=False)
+    ctx64.close()
+    prec = 1 if wl["opts"].get("precision") else 0
+    prof = mixed["prof"]
+    cats = {"precond": BYTES_PRECOND[prec] * nc, "spmv": BYTES_SPMV[prec] * nc}
+    dom = max(cats, key=lambda k: prof[k][0])
+    per_launch_ms = prof[dom][0] / max(prof[dom][1], 1)
+    achieved = cats[dom] / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    hist = mixed["hist"]
     line = {"metric": METRIC, "metric_full": METRIC_FULL, "value": value, "unit": METRIC,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None,
-            "dtype": "f32 system / f64 residual" if wl["opts"].get("precision") else "f64",
+            "vs_baseline": None, "dtype": "f32 system / f64 residual and update",
             "data": "synthetic",
             "config": {"workload": args.workload, "cells": nc, "faces": ctx.n_faces,
                        "parallelism": f"replicas{world}",
                        "l2": "flushed before every timed step (256 MB write)",
-                       "linear_iterations_per_step": float(lin.mean()),
+                       "linear_iterations_per_step": float(hist[:, 12].mean()),
                        "cfl_range": [float(hist[0, 10]), float(hist[-1, 10])]},
+            "fp64_plain": {"value": world * nc * args.steps / (plain["ms"] / 1e3),
+                           "ms_per_step": plain["ms"] / args.steps,
+                           "linear_iterations_per_step": float(plain["hist"][:, 12].mean()),
+                           "mixed_over_fp64": plain["ms"] / mixed["ms"]},
             "e2e": {"value": world * nc * args.steps / e2e_s, "unit": METRIC,
                     "h2d_bytes_per_step": 40 * nc, "d2h_bytes_per_step": 40 * nc},
-            "gpu_launches": c1["launches"] - c0["launches"], "clocks": clk}
+            "gpu_launches": mixed["launches"],
+            "roofline": {"kernel": {"precond": "block-ILU(0) sweeps (ilu_lower/upper_kernel)",
+                                    "spmv": "spmv_kernel"}[dom],
+                         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": traffic_from_profiles(dom, args.workload),
+                         "ms_per_launch": per_launch_ms, "bytes_per_launch": cats[dom],
+                         "category_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()}},
+            "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = implicit_cpu_baseline(wl)
     return line
 
 
@@ -314,7 +410,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="explicit_bump_72k", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="implicit_bump_2m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--converge", type=int, default=0,
                     help="implicit workloads: also solve to a 1e-8 residual drop (max steps)")

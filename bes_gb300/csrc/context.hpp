@@ -89,6 +89,21 @@ struct ImplicitBuffers {
 };
 }  // namespace bes
 
+namespace bes {
+// Optional event timing of the implicit path by kernel category (bes_profile).
+enum ProfCat { PROF_RESIDUAL = 0, PROF_JACOBIAN, PROF_ASSEMBLE, PROF_ILU_FACTOR, PROF_PRECOND,
+               PROF_SPMV, PROF_ORTHO, PROF_OTHER, PROF_NCAT };
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;                     // pairs: begin at 2k, end at 2k+1
+  int next = 0;                                      // next free pair
+  std::vector<std::pair<int, int>> pending;          // (category, pair)
+  int open_pair[PROF_NCAT];
+  double ms[PROF_NCAT] = {};
+  int64_t count[PROF_NCAT] = {};
+};
+}  // namespace bes
+
 struct bes_ctx {
   bes_options opt;
   bes::RefMesh ref;
@@ -130,9 +145,16 @@ struct bes_ctx {
   int64_t iters_since_reset = 0;  // graph launches since the history counter was reset
   bes::ImplicitBuffers imp;
   int64_t launches = 0;  // kernels launched by this context (graph nodes counted per launch)
+  bes::Profiler prof;
 };
 
 namespace bes {
 int check_nan_public(bes_ctx* ctx);   // synchronises; BES_ERR_NAN if a face flux was NaN
 int implicit_allocate(bes_ctx* ctx);  // buffers of the implicit path
+}  // namespace bes
+
+namespace bes {
+void prof_begin(bes_ctx* c, int cat);
+void prof_end(bes_ctx* c, int cat);
+void prof_collect(bes_ctx* c);  // after a synchronisation: accumulate finished pairs
 }  // namespace bes

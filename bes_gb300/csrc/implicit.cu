@@ -154,7 +154,9 @@ int precond_setup(const Sys<T>& S) {
   if (!uses_ilu(c)) return BES_OK;  // block Jacobi inverted during assembly
   int rc = ensure_ilu_graphs(S);
   if (rc) return rc;
+  prof_begin(c, PROF_ILU_FACTOR);
   IMP_TRY(c, cudaGraphLaunch(c->imp.factor_graph, S.s));
+  prof_end(c, PROF_ILU_FACTOR);
   c->launches += c->soa.n_stages;
   return BES_OK;
 }
@@ -168,6 +170,7 @@ int assemble(bes_ctx* c, double cfl, double* norms15) {
   const bes_options& o = c->opt;
   const int local = o.local_time_step;
   double* U = c->U[c->cur];
+  prof_begin(c, PROF_RESIDUAL);
   reset_dtmin_kernel<<<1, 1, 0, S.s>>>(c->dtmin);
   ++S.c->launches;
   cell_recon_kernel<true, false><<<nblk(m.nc, kBlock), kBlock, 0, S.s>>>(
@@ -176,19 +179,25 @@ int assemble(bes_ctx* c, double cfl, double* norms15) {
   face_flux_kernel<false><<<nblk(m.nf, kBlock), kBlock, 0, S.s>>>(m, c->prm, c->RS, c->rs_ld,
                                                                   c->FA, nullptr, c->nan_flag);
   ++S.c->launches;
+  prof_end(c, PROF_RESIDUAL);
   FaceLocal fl{c->imp.m_own, c->imp.m_nb};
+  prof_begin(c, PROF_JACOBIAN);
   face_jacobian_kernel<T><<<nblk(m.nf, 128), 128, 0, S.s>>>(
       m, c->prm, fl, U, c->dt, c->dtmin, local, o.jacobian_repeat, S.A, S.Dc);
   ++S.c->launches;
+  prof_end(c, PROF_JACOBIAN);
   const int nb = nblk(m.nc, 128);
+  prof_begin(c, PROF_ASSEMBLE);
   cell_assemble_kernel<T><<<nb, 128, 0, S.s>>>(m, c->FA, c->dt, c->dtmin, local,
                                                o.jacobian_repeat, S.Dc, S.A,
                                                uses_ilu(c) ? nullptr : S.Dinv,
                                                c->imp.rhs, S.b, c->imp.red);
   ++S.c->launches;
+  prof_end(c, PROF_ASSEMBLE);
   IMP_TRY(c, cudaGetLastError());
   double r[15];
   const int rc = reduce_to_host(c, 15, nb, 10, 1, r);
+  prof_collect(c);
   // norms15: L2 of the right-hand side [5], max of the right-hand side [5], L2 of R [5]
   for (int v = 0; v < 5; ++v) {
     norms15[v] = r[v];
@@ -235,13 +244,18 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
     g[0] = beta;
     int j = 0;
     while (j < mr && iter < maxiter) {
+      prof_begin(c, PROF_PRECOND);
       precond_apply(S, S.Vk(j), S.Z);
+      prof_end(c, PROF_PRECOND);
+      prof_begin(c, PROF_SPMV);
       spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.Z, nullptr, S.W);
+      prof_end(c, PROF_SPMV);
       ++S.c->launches;
       // classical Gram-Schmidt, two passes; coefficients stay on the device
       // (dev[0..31] first pass, dev[32..63] second pass, dev[64] |w|^2) and reach the host
       // once per iteration
       double* dev = c->imp.red_out;
+      prof_begin(c, PROF_ORTHO);
       launch_dots<T>(j + 1, G, S.s, S.V, S.N, S.W, S.N, red);
       reduce_rows_kernel<<<j + 1, 256, 0, S.s>>>(red, G, j + 1, 0, dev);
       launch_axpy<T>(j + 1, true, G, S.s, S.W, S.V, S.N, dev, S.N, red);
@@ -249,10 +263,12 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       launch_axpy<T>(j + 1, false, G, S.s, S.W, S.V, S.N, dev + 32, S.N, red);
       reduce_rows_kernel<<<1, 256, 0, S.s>>>(red, G, 1, 0, dev + 64);
       normalize_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(j + 1), S.W, dev + 64, S.N);
+      prof_end(c, PROF_ORTHO);
       S.c->launches += 7;
       double hbuf[65];
       IMP_TRY(c, cudaMemcpyAsync(hbuf, dev, sizeof(hbuf), cudaMemcpyDeviceToHost, S.s));
       IMP_TRY(c, cudaStreamSynchronize(S.s));
+      prof_collect(c);
       for (int i = 0; i <= j; ++i) {
         h[i] = hbuf[i];
         h2[i] = hbuf[32 + i];
@@ -336,7 +352,9 @@ int implicit_step(bes_ctx* c, double* hist) {
   double rel = 0.0;
   rc = gmres<T>(c, iters, rel);
   if (rc) return rc;
+  prof_begin(c, PROF_OTHER);
   state_update_kernel<T><<<kRedBlocks, 256, 0, c->stream>>>(c->U[c->cur], S.X, S.N);
+  prof_end(c, PROF_OTHER);
   ++c->launches;
   IMP_TRY(c, cudaGetLastError());
   for (int v = 0; v < 5; ++v) I.maxres[v] = norms[5 + v];
@@ -366,6 +384,44 @@ int implicit_step(bes_ctx* c, double* hist) {
 }  // namespace
 
 namespace bes {
+
+void prof_begin(bes_ctx* c, int cat) {
+  Profiler& P = c->prof;
+  if (!P.on) return;
+  if (P.next * 2 + 2 > (int)P.pool.size()) {
+    for (int q = 0; q < 64; ++q) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      P.pool.push_back(e);
+    }
+  }
+  const int pr = P.next++;
+  P.open_pair[cat] = pr;
+  cudaEventRecord(P.pool[2 * pr], c->stream);
+}
+
+void prof_end(bes_ctx* c, int cat) {
+  Profiler& P = c->prof;
+  if (!P.on) return;
+  const int pr = P.open_pair[cat];
+  cudaEventRecord(P.pool[2 * pr + 1], c->stream);
+  P.pending.push_back({cat, pr});
+}
+
+void prof_collect(bes_ctx* c) {
+  Profiler& P = c->prof;
+  if (!P.on) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto& q : P.pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, P.pool[2 * q.second], P.pool[2 * q.second + 1]) == cudaSuccess) {
+      P.ms[q.first] += ms;
+      P.count[q.first] += 1;
+    }
+  }
+  P.pending.clear();
+  P.next = 0;
+}
 
 int implicit_allocate(bes_ctx* c) {
   ImplicitBuffers& I = c->imp;
@@ -428,6 +484,23 @@ int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history) {
     if (rc) return rc;
   }
   IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  prof_collect(ctx);
+  return BES_OK;
+}
+
+int bes_profile(bes_ctx* ctx, int32_t enable, double* ms_out, int64_t* counts_out) {
+  if (!ctx) return BES_ERR_INVALID;
+  Profiler& P = ctx->prof;
+  prof_collect(ctx);
+  if (ms_out)
+    for (int k = 0; k < PROF_NCAT; ++k) ms_out[k] = P.ms[k];
+  if (counts_out)
+    for (int k = 0; k < PROF_NCAT; ++k) counts_out[k] = P.count[k];
+  for (int k = 0; k < PROF_NCAT; ++k) {
+    P.ms[k] = 0;
+    P.count[k] = 0;
+  }
+  P.on = enable != 0;
   return BES_OK;
 }
 

@@ -26,7 +26,7 @@ EXPORTED = [
     "bes_flux_batch", "bes_build_info", "bes_abi_sizes", "bes_host_geometry",
     "bes_explicit_enqueue", "bes_synchronize", "bes_stream", "bes_last_kernel_times",
     "bes_residual_norms_static", "bes_implicit_steps", "bes_implicit_assemble",
-    "bes_ilu_order", "bes_counters", "bes_wall_force",
+    "bes_ilu_order", "bes_counters", "bes_wall_force", "bes_profile",
 ]
 
 
@@ -105,6 +105,7 @@ def load(path: str = LIB_PATH):
     L.bes_ilu_order.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_counters.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_wall_force.argtypes = [P, D]
+    L.bes_profile.argtypes = [P, ctypes.c_int32, D, ctypes.POINTER(ctypes.c_int64)]
     L.bes_residual_norms_static.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
     I64 = ctypes.POINTER(ctypes.c_int64)
@@ -320,6 +321,17 @@ class Context:
         self._check(load().bes_implicit_assemble(self.h, float(cfl), _d(rhs), _d(blocks),
                                                  ctypes.byref(nb)))
         return dict(rhs=rhs, blocks=blocks)
+
+    PROFILE_CATEGORIES = ("residual", "jacobian", "assemble", "ilu_factor", "precond",
+                          "spmv", "gram_schmidt", "update")
+
+    def profile(self, enable: bool = True) -> dict:
+        """Turn implicit-path event timing on/off; returns what accumulated since the last call
+        as {category: (ms, count)}."""
+        ms = np.zeros(8)
+        cnt = np.zeros(8, np.int64)
+        self._check(load().bes_profile(self.h, int(enable), _d(ms), _i(cnt)))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.PROFILE_CATEGORIES)}
 
     def wall_force(self) -> np.ndarray:
         f = np.zeros(3)

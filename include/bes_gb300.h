@@ -145,6 +145,14 @@ int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history);
  * src/CoefficientMatrix.cpp:141-160).  Pass NULL arrays to query n_blocks. */
 int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks, int64_t* n_blocks);
 
+/* Event timing of the implicit path by kernel category (diagnostics for benchmarking).
+ * enable 1 turns timing on (an event pair around every category's work, read back at the
+ * step's synchronisation points), 0 off.  Returns (and resets) the accumulated milliseconds
+ * and launch-group counts since the previous call: ms_out / counts_out [8] = residual (cell
+ * sweep + face fluxes), Jacobians, assembly, ILU factorisation, preconditioner application,
+ * matrix-vector products, Gram-Schmidt (dots, updates, normalisation), state update. */
+int bes_profile(bes_ctx* ctx, int32_t enable, double* ms_out, int64_t* counts_out);
+
 /* The block-ILU(0) factorisation order (reference cell ids, colour by colour). */
 int bes_ilu_order(bes_ctx* ctx, int64_t* order);
 

@@ -133,3 +133,27 @@ def test_ilu_orders_match_oracle(linear_solver):
     assert np.array_equal(h[:, 12], ho[:, 12])
     assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
     assert rel_err(ctx.get_state(), O.get_state()) <= 1e-9
+
+
+@pytest.mark.gpu
+def test_profile_counts_follow_the_iterations():
+    """Event timing by kernel category: one preconditioner application, one SpMV and one
+    Gram-Schmidt pass per linear iteration (GMRES applies the preconditioner once more per
+    restart cycle to form the solution, which is not timed), one residual and one assembly per
+    step; timing off leaves the results unchanged."""
+    mesh = meshgen.bump_channel(24, 8, 6, 0.08)
+    kw = dict(solver_type=1, local_time_step=1, courant_num=10.0, freestream_mach=(0.84, 0, 0),
+              linear_solver=1, linear_solver_tol=1e-2, linear_solver_max_iter=300,
+              cfl_ramp_steps=8, cfl_ramp_start=10.0, cfl_ramp_end=500.0)
+    a = context(mesh, **kw)
+    b = context(mesh, **kw)
+    a.profile(True)
+    ha = a.implicit_steps(6)
+    p = a.profile(False)
+    hb = b.implicit_steps(6)
+    assert np.array_equal(ha, hb)
+    its = int(ha[:, 12].sum())
+    assert p["residual"][1] == 6 and p["assemble"][1] == 6 and p["ilu_factor"][1] == 6
+    assert p["spmv"][1] == its and p["gram_schmidt"][1] == its and p["precond"][1] == its
+    assert all(v[0] > 0 for k, v in p.items() if v[1])
+    assert a.profile(False)["spmv"] == (0.0, 0)
