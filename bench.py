@@ -60,6 +60,15 @@ WORKLOADS = {
                                              gmres_restart=30, cfl_ramp_steps=50,
                                              cfl_ramp_start=10.0, cfl_ramp_end=1000.0,
                                              precision=1)),
+    # the same scheme on the 120x40x18-hex channel (518,400 tets): a profiling size whose
+    # Krylov basis (31 vectors of 10 MB) still exceeds L2
+    "implicit_bump_518k": dict(kind="implicit", mesh=("bump", 120, 40, 18, 0.08),
+                               opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
+                                         freestream_mach=(0.84, 0.0, 0.0), linear_solver=1,
+                                         linear_solver_tol=1e-2, linear_solver_max_iter=300,
+                                         gmres_restart=30, cfl_ramp_steps=50,
+                                         cfl_ramp_start=10.0, cfl_ramp_end=1000.0,
+                                         precision=1)),
     "implicit_bump_2m_fp64": dict(kind="implicit", mesh=("bump", 200, 60, 30, 0.08),
                                   opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
                                             freestream_mach=(0.84, 0.0, 0.0), linear_solver=1,

@@ -480,6 +480,7 @@ int bes_counters(const bes_ctx* ctx, int64_t* out) {
   out[1] = ctx->iterations_done;
   out[2] = ctx->imp.step_count;
   out[3] = ctx->imp.total_lin_iters;
+  out[4] = ctx->imp.gs_second_passes;
   return BES_OK;
 }
 

@@ -85,6 +85,7 @@ struct ImplicitBuffers {
   int64_t step_count = 0;
   int last_iters = 0;
   int64_t total_lin_iters = 0;
+  int64_t gs_second_passes = 0;  // Arnoldi steps that needed a second Gram-Schmidt pass
   double last_err = 0;
 };
 }  // namespace bes

@@ -37,6 +37,8 @@ int imp_malloc(bes_ctx* c, void** p, size_t bytes) {
   return BES_OK;
 }
 
+inline int64_t basis_stride(int64_t nc) { return (5 * nc + 63) / 64 * 64; }
+
 template <class T>
 struct Sys {
   bes_ctx* c;
@@ -56,6 +58,7 @@ struct Sys {
     ImplicitBuffers& I = ctx->imp;
     nc = ctx->soa.nc;
     N = 5LL * nc;
+    ldv = basis_stride(nc);
     A = (T*)I.A;
     LU = (T*)I.LU;
     Dinv = (T*)I.Dinv;
@@ -67,7 +70,8 @@ struct Sys {
     X = (T*)I.X;
     s = ctx->stream;
   }
-  T* Vk(int k) const { return V + (int64_t)k * N; }
+  int64_t ldv;  // stride of the Krylov basis: N rounded up to 64 elements (16-byte loads)
+  T* Vk(int k) const { return V + (int64_t)k * ldv; }
 };
 
 // reduce rows of c->imp.red and copy them to the host
@@ -207,7 +211,7 @@ int assemble(bes_ctx* c, double cfl, double* norms15) {
   return rc;
 }
 
-// Right-preconditioned GMRES(m), x0 = 0, classical Gram-Schmidt with one re-orthogonalisation
+// Right-preconditioned GMRES(m), x0 = 0, classical Gram-Schmidt with a conditional second
 // pass, Givens rotations; stops when |g_{j+1}| <= tol |b| (AMGCL gmres.hpp:163,214 semantics).
 template <class T>
 int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
@@ -230,7 +234,7 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
   rel_out = 0.0;
   if (norm_b == 0.0) return BES_OK;
   const double eps = tol * norm_b;
-  std::vector<double> H((mr + 1) * mr, 0.0), cs(mr), sn(mr), g(mr + 1), h(mr + 1), h2(mr + 1), y(mr);
+  std::vector<double> H((mr + 1) * mr, 0.0), cs(mr), sn(mr), g(mr + 1), y(mr);
   int iter = 0;
   double norm_r = norm_b;
   scale_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.b, 1.0, S.N);  // r = b
@@ -251,32 +255,29 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.Z, nullptr, S.W);
       prof_end(c, PROF_SPMV);
       ++S.c->launches;
-      // classical Gram-Schmidt, two passes; coefficients stay on the device
-      // (dev[0..31] first pass, dev[32..63] second pass, dev[64] |w|^2) and reach the host
-      // once per iteration
+      // classical Gram-Schmidt with a conditional second pass (gs_* kernels); the
+      // coefficients stay on the device and reach the host once per iteration
       double* dev = c->imp.red_out;
+      const int nv = j + 1;
       prof_begin(c, PROF_ORTHO);
-      launch_dots<T>(j + 1, G, S.s, S.V, S.N, S.W, S.N, red);
-      reduce_rows_kernel<<<j + 1, 256, 0, S.s>>>(red, G, j + 1, 0, dev);
-      launch_axpy<T>(j + 1, true, G, S.s, S.W, S.V, S.N, dev, S.N, red);
-      reduce_rows_kernel<<<j + 1, 256, 0, S.s>>>(red, G, j + 1, 0, dev + 32);
-      launch_axpy<T>(j + 1, false, G, S.s, S.W, S.V, S.N, dev + 32, S.N, red);
-      reduce_rows_kernel<<<1, 256, 0, S.s>>>(red, G, 1, 0, dev + 64);
-      normalize_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(j + 1), S.W, dev + 64, S.N);
+      launch_gs_dots<T>(nv, G, S.s, S.V, S.ldv, S.W, S.N, red);
+      reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev);
+      gs_decide_kernel<<<1, 32, 0, S.s>>>(dev, nv, 1);
+      launch_gs_update<T, GS_FINAL1>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, S.N, red);
+      launch_gs_update<T, GS_REORTH>(nv, G, S.s, nullptr, S.W, S.V, S.ldv, dev, S.N, red);
+      reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev + kGsH2);
+      gs_decide_kernel<<<1, 32, 0, S.s>>>(dev, nv, 2);
+      launch_gs_update<T, GS_FINAL2>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, S.N, red);
       prof_end(c, PROF_ORTHO);
-      S.c->launches += 7;
-      double hbuf[65];
+      S.c->launches += 8;
+      double hbuf[kGsScalars];
       IMP_TRY(c, cudaMemcpyAsync(hbuf, dev, sizeof(hbuf), cudaMemcpyDeviceToHost, S.s));
       IMP_TRY(c, cudaStreamSynchronize(S.s));
       prof_collect(c);
-      for (int i = 0; i <= j; ++i) {
-        h[i] = hbuf[i];
-        h2[i] = hbuf[32 + i];
-      }
-      const double hn2 = hbuf[64];
-      for (int i = 0; i <= j; ++i) H[i * mr + j] = h[i] + h2[i];
-      const double hn = std::sqrt(hn2);
-      H[(j + 1) * mr + j] = hn;
+      const bool second = hbuf[kGsFlag] != 0.0;
+      if (second) ++c->imp.gs_second_passes;
+      for (int i = 0; i <= j; ++i) H[i * mr + j] = hbuf[i] + (second ? hbuf[kGsH2 + i] : 0.0);
+      H[(j + 1) * mr + j] = hbuf[kGsNorm];
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * H[i * mr + j] + sn[i] * H[(i + 1) * mr + j];
         H[(i + 1) * mr + j] = -sn[i] * H[i * mr + j] + cs[i] * H[(i + 1) * mr + j];
@@ -300,7 +301,7 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       y[i] = s / H[i * mr + i];
     }
     IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, S.s));
-    lincomb_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.N, j, c->imp.coef, S.N);
+    lincomb_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.ldv, j, c->imp.coef, S.N);
     ++S.c->launches;
     precond_apply(S, S.W, S.Z);
     add_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.Z, S.N);
@@ -446,7 +447,7 @@ int implicit_allocate(bes_ctx* c) {
   if (uses_ilu(c)) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
   rc |= imp_malloc(c, &I.b, N * I.tsize);
-  rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * N * I.tsize);
+  rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * basis_stride(nc) * I.tsize);
   rc |= imp_malloc(c, &I.Z, N * I.tsize);
   rc |= imp_malloc(c, &I.W, N * I.tsize);
   rc |= imp_malloc(c, &I.X, N * I.tsize);

@@ -468,58 +468,169 @@ __device__ __forceinline__ void block_reduce_store(A (&acc_in)[NV], double* part
   }
 }
 
-// Partial dot products V_k . w for k < NV in one pass over the vectors (each element of w
-// and of every V_k is read once).
+// ---- Gram-Schmidt of the Arnoldi step -------------------------------------------------
+// Classical Gram-Schmidt with a conditional second pass (the oracle's linsolve.hpp gmres
+// states the same algorithm):
+//   pass 1   h = V^T w and |w|^2 in one read of V and w (gs_dots_kernel);
+//   decide   |w - V h|^2 = |w|^2 - |h|^2 (Pythagoras); a second pass runs only when this
+//            is <= kReorthTheta2 |w|^2 (gs_decide_kernel, on the device, so the host is not
+//            asked);
+//   no second pass: V_{j+1} = (w - V h) / sqrt(|w|^2 - |h|^2) in one more read of V and w
+//            (gs_update_kernel<FINAL1>);
+//   second pass: w -= V h with V^T w and |w|^2 of the result in the same read
+//            (gs_update_kernel<REORTH>), then V_{j+1} = (w - V h2) / norm (<FINAL2>).
+// The kernels of the path not taken return at once.  Device scalars (dev = red_out):
+//   dev[0..nv-1] h, dev[nv] |w|^2; dev[kGsH2 + k] h2, dev[kGsH2 + nv] |w'|^2;
+//   dev[kGsFlag] 1 if the second pass runs, dev[kGsInv] 1/h_{j+1,j} (0: leave V_{j+1}),
+//   dev[kGsNorm] h_{j+1,j}.
+constexpr double kReorthTheta2 = 1.0 / 16.0;
+constexpr int kGsH2 = 40, kGsFlag = 80, kGsInv = 81, kGsNorm = 82, kGsScalars = 83;
+
+// 16-byte unit of the vector kernels; the Krylov basis stride is a multiple of it
+template <class T>
+struct alignas(16) Pack16 {
+  static constexpr int W = 16 / sizeof(T);
+  T v[W];
+};
+
+// Pass 1: partial V_k . w (rows k < NV) and |w|^2 (row NV).
 template <class T, int NV>
-__global__ void __launch_bounds__(256) dots_kernel(const T* __restrict__ V, int64_t ldv,
-                                                   const T* __restrict__ w, int64_t N,
-                                                   double* __restrict__ partials) {
+__global__ void __launch_bounds__(256) gs_dots_kernel(const T* __restrict__ V, int64_t ldv,
+                                                      const T* __restrict__ w, int64_t N,
+                                                      double* __restrict__ partials) {
   typedef typename AccType<T>::type A;
-  A acc[NV];
+  typedef Pack16<T> P;
+  constexpr int W = P::W;
+  A acc[NV + 1];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) acc[k] = A(0);
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const A wv = (A)w[idx];
+  for (int k = 0; k <= NV; ++k) acc[k] = A(0);
+  const int64_t ng = N / W;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const P wv = reinterpret_cast<const P*>(w)[g];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] += (A)V[(int64_t)k * ldv + idx] * wv;
+    for (int e = 0; e < W; ++e) acc[NV] += (A)wv.v[e] * (A)wv.v[e];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const P vk = reinterpret_cast<const P*>(V + (int64_t)k * ldv)[g];
+#pragma unroll
+      for (int e = 0; e < W; ++e) acc[k] += (A)vk.v[e] * (A)wv.v[e];
+    }
   }
-  block_reduce_store<NV, A>(acc, partials);
+  if (blockIdx.x == 0 && threadIdx.x < N - ng * W) {  // the ragged tail, < W elements
+    const int64_t i = ng * W + threadIdx.x;
+    const A x = (A)w[i];
+    acc[NV] += x * x;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] += (A)V[(int64_t)k * ldv + i] * x;
+  }
+  block_reduce_store<NV + 1, A>(acc, partials);
 }
 
-// w -= sum_k h_k V_k (k < NV) in one pass; then DOTS: partial V_k . w_new, or else partial
-// |w_new|^2 (row 0).  Every element of w and of every V_k is read once.
-template <class T, int NV, bool DOTS>
-__global__ void __launch_bounds__(256) axpy_reduce_kernel(T* __restrict__ w, const T* __restrict__ V,
-                                                          int64_t ldv, const double* __restrict__ h,
-                                                          int64_t N, double* __restrict__ partials) {
+// Decide after a reduction: stage 1 (after pass 1) sets the second-pass flag and, without a
+// second pass, 1/h_{j+1,j}; stage 2 (after pass 2) sets 1/h_{j+1,j} from the second pass.
+static __global__ void gs_decide_kernel(double* __restrict__ dev, int nv, int stage) {
+  if (threadIdx.x != 0) return;
+  if (stage == 1) {
+    const double nw2 = dev[nv];
+    double s = 0.0;
+    for (int k = 0; k < nv; ++k) s += dev[k] * dev[k];
+    const double est = nw2 - s;
+    const bool reorth = !(est > kReorthTheta2 * nw2);
+    dev[kGsFlag] = reorth ? 1.0 : 0.0;
+    const double hn = reorth ? 0.0 : sqrt(est);
+    dev[kGsNorm] = hn;
+    dev[kGsInv] = hn > 0.0 ? 1.0 / hn : 0.0;
+  } else {
+    if (dev[kGsFlag] == 0.0) return;
+    const double nw2 = dev[kGsH2 + nv];
+    double s = 0.0;
+    for (int k = 0; k < nv; ++k) s += dev[kGsH2 + k] * dev[kGsH2 + k];
+    const double e2 = nw2 - s;
+    const double hn = e2 > 0.0 ? sqrt(e2) : 0.0;
+    dev[kGsNorm] = hn;
+    dev[kGsInv] = hn > 0.0 ? 1.0 / hn : 0.0;
+  }
+}
+
+enum GsMode { GS_FINAL1 = 0, GS_REORTH = 1, GS_FINAL2 = 2 };
+
+// FINAL1 / FINAL2: out = (w - sum_k c_k V_k) * dev[kGsInv] with c = h (FINAL1, runs without
+// a second pass) or h2 (FINAL2, runs with one).  REORTH: w -= sum_k h_k V_k in place, with
+// partial V_k . w (rows k < NV) and |w|^2 (row NV) of the result.
+template <class T, int NV, int MODE>
+__global__ void __launch_bounds__(256) gs_update_kernel(T* __restrict__ out, T* w,
+                                                        const T* __restrict__ V, int64_t ldv,
+                                                        const double* __restrict__ dev,
+                                                        int64_t N, double* __restrict__ partials) {
   typedef typename AccType<T>::type A;
-  A hs[NV];
+  typedef Pack16<T> P;
+  constexpr int W = P::W;
+  const bool second = dev[kGsFlag] != 0.0;
+  const bool runs = MODE == GS_FINAL1 ? !second : second;
+  if (!runs) return;
+  const double* coef = MODE == GS_FINAL2 ? dev + kGsH2 : dev;
+  const double invd = dev[kGsInv];
+  if (MODE != GS_REORTH && invd == 0.0) return;  // h_{j+1,j} = 0: V_{j+1} is not used
+  const A inv = (A)invd;
+  A c[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) hs[k] = (A)h[k];
-  constexpr int NA = DOTS ? NV : 1;
+  for (int k = 0; k < NV; ++k) c[k] = (A)coef[k];
+  constexpr int NA = MODE == GS_REORTH ? NV + 1 : 1;
   A acc[NA];
 #pragma unroll
   for (int k = 0; k < NA; ++k) acc[k] = A(0);
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    T v[NV];
-    A x = (A)w[idx];
+  const int64_t ng = N / W;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const P wv = reinterpret_cast<const P*>(w)[g];
+    A x[W];
+#pragma unroll
+    for (int e = 0; e < W; ++e) x[e] = (A)wv.v[e];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      v[k] = V[(int64_t)k * ldv + idx];
-      x -= hs[k] * (A)v[k];
-    }
-    const T xt = (T)x;
-    w[idx] = xt;
-    if (DOTS) {
+      const P vk = reinterpret_cast<const P*>(V + (int64_t)k * ldv)[g];
 #pragma unroll
-      for (int k = 0; k < NA; ++k) acc[k] += (A)v[k] * (A)xt;
+      for (int e = 0; e < W; ++e) x[e] -= c[k] * (A)vk.v[e];
+    }
+    P o;
+    if (MODE == GS_REORTH) {
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        o.v[e] = (T)x[e];
+        acc[NV] += (A)o.v[e] * (A)o.v[e];
+      }
+      // the second pass is rare: V is read again (from L2) for its dot products rather than
+      // held in registers
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        const P vk = reinterpret_cast<const P*>(V + (int64_t)k * ldv)[g];
+#pragma unroll
+        for (int e = 0; e < W; ++e) acc[k] += (A)vk.v[e] * (A)o.v[e];
+      }
+      reinterpret_cast<P*>(w)[g] = o;
     } else {
-      acc[0] += (A)xt * (A)xt;
+#pragma unroll
+      for (int e = 0; e < W; ++e) o.v[e] = (T)(x[e] * inv);
+      reinterpret_cast<P*>(out)[g] = o;
     }
   }
-  block_reduce_store<NA, A>(acc, partials);
+  if (blockIdx.x == 0 && threadIdx.x < N - ng * W) {  // the ragged tail
+    const int64_t i = ng * W + threadIdx.x;
+    A x = (A)w[i];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) x -= c[k] * (A)V[(int64_t)k * ldv + i];
+    if (MODE == GS_REORTH) {
+      const T xt = (T)x;
+      w[i] = xt;
+      acc[NV] += (A)xt * (A)xt;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] += (A)V[(int64_t)k * ldv + i] * (A)xt;
+    } else {
+      out[i] = (T)(x * inv);
+    }
+  }
+  if (MODE == GS_REORTH) block_reduce_store<NA, A>(acc, partials);
 }
 
 // Launch helpers dispatching the vector count to a compile-time constant (1..32).
@@ -528,36 +639,26 @@ __global__ void __launch_bounds__(256) axpy_reduce_kernel(T* __restrict__ w, con
   X(17) X(18) X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27) X(28) X(29) X(30) X(31) X(32)
 
 template <class T>
-void launch_dots(int nvec, int G, cudaStream_t s, const T* V, int64_t ldv, const T* w, int64_t N,
-                 double* partials) {
+void launch_gs_dots(int nvec, int G, cudaStream_t s, const T* V, int64_t ldv, const T* w,
+                    int64_t N, double* partials) {
   switch (nvec) {
 #define BES_DOTS_CASE(n) \
-  case n: dots_kernel<T, n><<<G, 256, 0, s>>>(V, ldv, w, N, partials); break;
+  case n: gs_dots_kernel<T, n><<<G, 256, 0, s>>>(V, ldv, w, N, partials); break;
     BES_NV_CASES(BES_DOTS_CASE)
 #undef BES_DOTS_CASE
     default: break;
   }
 }
 
-template <class T>
-void launch_axpy(int nvec, bool dots, int G, cudaStream_t s, T* w, const T* V, int64_t ldv,
-                 const double* h, int64_t N, double* partials) {
-  if (dots) {
-    switch (nvec) {
-#define BES_AXPY_CASE(n) \
-  case n: axpy_reduce_kernel<T, n, true><<<G, 256, 0, s>>>(w, V, ldv, h, N, partials); break;
-      BES_NV_CASES(BES_AXPY_CASE)
-#undef BES_AXPY_CASE
-      default: break;
-    }
-  } else {
-    switch (nvec) {
-#define BES_AXPY_CASE(n) \
-  case n: axpy_reduce_kernel<T, n, false><<<G, 256, 0, s>>>(w, V, ldv, h, N, partials); break;
-      BES_NV_CASES(BES_AXPY_CASE)
-#undef BES_AXPY_CASE
-      default: break;
-    }
+template <class T, int MODE>
+void launch_gs_update(int nvec, int G, cudaStream_t s, T* out, T* w, const T* V, int64_t ldv,
+                      const double* dev, int64_t N, double* partials) {
+  switch (nvec) {
+#define BES_UPD_CASE(n) \
+  case n: gs_update_kernel<T, n, MODE><<<G, 256, 0, s>>>(out, w, V, ldv, dev, N, partials); break;
+    BES_NV_CASES(BES_UPD_CASE)
+#undef BES_UPD_CASE
+    default: break;
   }
 }
 
@@ -566,21 +667,6 @@ __global__ void __launch_bounds__(256) scale_kernel(T* __restrict__ out, const T
                                                     double s, int64_t N) {
   typedef typename AccType<T>::type A;
   const A sa = (A)s;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
-       idx += (int64_t)gridDim.x * blockDim.x)
-    out[idx] = (T)((A)in[idx] * sa);
-}
-
-// out = in / sqrt(*norm2) (the new Arnoldi vector), left untouched when the norm is zero
-template <class T>
-__global__ void __launch_bounds__(256) normalize_kernel(T* __restrict__ out,
-                                                        const T* __restrict__ in,
-                                                        const double* __restrict__ norm2,
-                                                        int64_t N) {
-  typedef typename AccType<T>::type A;
-  const double n2 = *norm2;
-  if (!(n2 > 0.0)) return;
-  const A sa = (A)(1.0 / sqrt(n2));
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x)
     out[idx] = (T)((A)in[idx] * sa);

@@ -339,10 +339,11 @@ class Context:
         return f
 
     def counters(self) -> dict:
-        out = np.zeros(4, np.int64)
+        out = np.zeros(5, np.int64)
         self._check(load().bes_counters(self.h, _i(out)))
         return dict(launches=int(out[0]), explicit_iterations=int(out[1]),
-                    implicit_steps=int(out[2]), linear_iterations=int(out[3]))
+                    implicit_steps=int(out[2]), linear_iterations=int(out[3]),
+                    gram_schmidt_second_passes=int(out[4]))
 
     def ilu_order(self) -> np.ndarray:
         o = np.zeros(self.n_cells, np.int64)

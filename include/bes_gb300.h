@@ -196,7 +196,8 @@ int bes_residual_norms_static(const double* residual, int64_t n_cells, double* n
 int bes_wall_force(bes_ctx* ctx, double* force);
 
 /* Counters of the context: out[0] kernels launched (graph kernel nodes counted per graph
- * launch), out[1] explicit iterations, out[2] implicit steps, out[3] linear iterations. */
+ * launch), out[1] explicit iterations, out[2] implicit steps, out[3] linear iterations,
+ * out[4] linear iterations whose Gram-Schmidt step needed the second pass.  out [5]. */
 int bes_counters(const bes_ctx* ctx, int64_t* out);
 
 /* Library build identification (e.g. "sm_103a"). */

@@ -10,7 +10,8 @@
 //     row by row in a caller-given cell order (IKJ variant).  The GPU processes the same
 //     order colour by colour, which is the same sequence of row operations.
 // GMRES is right preconditioned, restarted every m iterations, x0 = 0, classical
-// Gram-Schmidt with one re-orthogonalisation pass, Givens rotations, and the stopping test
+// Gram-Schmidt with a second (re-orthogonalisation) pass only where the first one cancelled
+// most of the new vector (see kReorthTheta2), Givens rotations, and the stopping test
 // |g_{j+1}| <= tol*|b| of AMGCL's gmres.hpp:163,214 (tol is relative, which is what the
 // reference's LINEAR_SOLVER_ABS_TOL key really sets).
 #pragma once
@@ -23,6 +24,9 @@ namespace besla {
 
 constexpr int NB = 5;             // block size: 5 conserved variables
 constexpr int NB2 = NB * NB;
+// Second Gram-Schmidt pass when |w - V h|^2 <= kReorthTheta2 |w|^2, i.e. when the first pass
+// cancelled 3/4 or more of |w| (two or more leading bits).
+constexpr double kReorthTheta2 = 1.0 / 16.0;
 
 // Block CSR: block row i owns blocks [row[i], row[i+1]); col[k] is the block column.
 struct BlockCsr {
@@ -225,20 +229,42 @@ inline GmresResult gmres(const BlockCsr& A, const Preconditioner& M, const doubl
     for (; j < restart && iter < maxiter; ++j, ++iter) {
       M.apply(&V[(int64_t)j * N], Z.data());
       bcsr_spmv(A, Z.data(), W.data());
-      // classical Gram-Schmidt, two passes
-      for (int pass = 0; pass < 2; ++pass) {
-        std::vector<double> h(j + 1);
-        for (int i = 0; i <= j; ++i) h[i] = dot(&V[(int64_t)i * N], W.data(), N);
+      // classical Gram-Schmidt: h = V^T w, w -= V h; the norm of the result follows from
+      // Pythagoras, |w - V h|^2 = |w|^2 - |h|^2, unless that estimate shows that more than
+      // 1 - sqrt(kReorthTheta2) of |w| cancelled, in which case a second pass orthogonalises
+      // again and the norm comes from the second pass's own Pythagoras step
+      std::vector<double> h(j + 1), h2(j + 1, 0.0);
+      for (int i = 0; i <= j; ++i) h[i] = dot(&V[(int64_t)i * N], W.data(), N);
+      const double nw2 = dot(W.data(), W.data(), N);
+      double s1 = 0.0;
+      for (int i = 0; i <= j; ++i) s1 += h[i] * h[i];
+      const double est = nw2 - s1;
+      const bool reorth = !(est > kReorthTheta2 * nw2);
+      for (int i = 0; i <= j; ++i) {
+        const double* vi = &V[(int64_t)i * N];
+        for (int64_t q = 0; q < N; ++q) W[q] -= h[i] * vi[q];
+      }
+      double hn = 0.0;
+      if (reorth) {
+        for (int i = 0; i <= j; ++i) h2[i] = dot(&V[(int64_t)i * N], W.data(), N);
+        const double nw2b = dot(W.data(), W.data(), N);
+        double s2 = 0.0;
+        for (int i = 0; i <= j; ++i) s2 += h2[i] * h2[i];
         for (int i = 0; i <= j; ++i) {
           const double* vi = &V[(int64_t)i * N];
-          for (int64_t q = 0; q < N; ++q) W[q] -= h[i] * vi[q];
-          H[i * restart + j] = (pass == 0 ? 0.0 : H[i * restart + j]) + h[i];
+          for (int64_t q = 0; q < N; ++q) W[q] -= h2[i] * vi[q];
         }
+        const double e2 = nw2b - s2;
+        hn = e2 > 0.0 ? std::sqrt(e2) : 0.0;
+      } else {
+        hn = std::sqrt(est);
       }
-      const double hn = std::sqrt(dot(W.data(), W.data(), N));
+      for (int i = 0; i <= j; ++i) H[i * restart + j] = h[i] + h2[i];
       H[(j + 1) * restart + j] = hn;
-      if (hn != 0.0)
-        for (int64_t q = 0; q < N; ++q) V[(int64_t)(j + 1) * N + q] = W[q] / hn;
+      if (hn != 0.0) {
+        const double inv = 1.0 / hn;
+        for (int64_t q = 0; q < N; ++q) V[(int64_t)(j + 1) * N + q] = W[q] * inv;
+      }
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * H[i * restart + j] + sn[i] * H[(i + 1) * restart + j];
         H[(i + 1) * restart + j] = -sn[i] * H[i * restart + j] + cs[i] * H[(i + 1) * restart + j];
