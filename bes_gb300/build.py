@@ -38,8 +38,9 @@ def _headers():
 
 
 def _compile(src: str, obj: str, verbose_ptxas: bool) -> str:
+    # host code without FMA contraction, so that x86 and Arm hosts compute the same geometry
     flags = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-             "-I" + os.path.join(ROOT, "include")]
+             "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
     if src.endswith(".cu"):
         flags += ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
         if verbose_ptxas:

@@ -350,6 +350,47 @@ extern "C" void bes_mesh_free(bes_mesh_arrays* m) {
 extern "C" void bes_abi_sizes(int64_t* out) {
   out[0] = (int64_t)sizeof(bes_options);
   out[1] = (int64_t)sizeof(bes_mesh_arrays);
+  out[2] = (int64_t)sizeof(bes_output);
+}
+
+extern "C" int bes_output_from_besi(const char* path, bes_output* out, char* err,
+                                    size_t err_cap) {
+  if (!path || !out) return BES_ERR_INVALID;
+  bes_output_default(out);
+  std::ifstream in(path);
+  if (!in) {
+    set_err(err, err_cap, std::string("cannot open ") + path);
+    return BES_ERR_CONFIG;
+  }
+  std::string line;
+  int lineno = 0;
+  while (std::getline(in, line)) {
+    ++lineno;
+    std::vector<std::string> kv = split(line.substr(0, line.find("//")), "=");
+    const std::string& key = kv[0];
+    if (key.empty()) continue;
+    const std::string arg = split(kv.size() > 1 ? kv[1] : "", ",")[0];
+    auto bad = [&](const std::string& m) {
+      set_err(err, err_cap, "line " + std::to_string(lineno) + ": " + m);
+      return BES_ERR_CONFIG;
+    };
+    if (key == "OUTPUT_FOLDER") {
+      std::snprintf(out->folder, sizeof(out->folder), "%s", arg.c_str());
+    } else if (key == "OUTPUT_FORMAT") {
+      if (arg == "VTK") out->format = BES_OUTPUT_VTK;
+      else if (arg == "CSV") out->format = BES_OUTPUT_CSV;
+      else return bad("Output format not supported");
+    } else if (key == "OUTPUT_SLIP_WALL") {
+      if (arg == "YES") out->slip_wall = 1;
+      else if (arg == "NO") out->slip_wall = 0;
+      else return bad("Output slip wall format not supported");
+    } else if (key == "SAVE_INTERVAL") {
+      double x;
+      if (!to_num(arg, x) || x < 0) return bad("bad SAVE_INTERVAL");
+      out->save_interval = (int64_t)x;
+    }
+  }
+  return BES_OK;
 }
 
 extern "C" int bes_host_geometry(const bes_mesh_arrays* mesh, int32_t muscl_face_vector,

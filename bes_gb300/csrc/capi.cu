@@ -189,6 +189,8 @@ int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** ou
     return BES_ERR_MESH;
   }
   build_soa(ctx->ref, opt->venkatakrishnan_factor, opt->muscl_face_vector != 0, true, ctx->soa);
+  ctx->nodes.assign(mesh->nodes, mesh->nodes + mesh->n_nodes * 3);
+  ctx->tets.assign(mesh->tets, mesh->tets + mesh->n_tets * 4);
   const SoaMesh& S = ctx->soa;
   bes_ctx* c = ctx.get();
   BES_CUDA_TRY(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));

@@ -108,6 +108,8 @@ struct Profiler {
 struct bes_ctx {
   bes_options opt;
   bes::RefMesh ref;
+  std::vector<double> nodes;  // the mesh arrays as given (the VTK writer's points and cells)
+  std::vector<int64_t> tets;
   bes::SoaMesh soa;
   bes::DevMesh dm;
   bes::Params prm;

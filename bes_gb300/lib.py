@@ -27,7 +27,10 @@ EXPORTED = [
     "bes_explicit_enqueue", "bes_synchronize", "bes_stream", "bes_last_kernel_times",
     "bes_residual_norms_static", "bes_implicit_steps", "bes_implicit_assemble",
     "bes_ilu_order", "bes_counters", "bes_wall_force", "bes_profile",
+    "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
 ]
+
+OUTPUT_VTK, OUTPUT_CSV, OUTPUT_SLIP_WALL_CSV = 0, 1, 2
 
 
 class BesError(RuntimeError):
@@ -41,6 +44,13 @@ class MeshArrays(ctypes.Structure):
                 ("n_btris", ctypes.c_int64), ("btris", ctypes.POINTER(ctypes.c_int64)),
                 ("btags", ctypes.POINTER(ctypes.c_int32)), ("n_tets", ctypes.c_int64),
                 ("tets", ctypes.POINTER(ctypes.c_int64))]
+
+
+class Output(ctypes.Structure):
+    """bes_output: the .besi output keys."""
+    _fields_ = [("folder", ctypes.c_char * 1024), ("format", ctypes.c_int32),
+                ("slip_wall", ctypes.c_int32), ("save_interval", ctypes.c_int64),
+                ("verbose", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Options(ctypes.Structure):
@@ -108,6 +118,15 @@ def load(path: str = LIB_PATH):
     L.bes_profile.argtypes = [P, ctypes.c_int32, D, ctypes.POINTER(ctypes.c_int64)]
     L.bes_residual_norms_static.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+    L.bes_output_default.argtypes = [ctypes.POINTER(Output)]
+    L.bes_output_default.restype = None
+    L.bes_output_from_besi.argtypes = [ctypes.c_char_p, ctypes.POINTER(Output), ctypes.c_char_p,
+                                       ctypes.c_size_t]
+    L.bes_write.argtypes = [P, ctypes.c_char_p, ctypes.c_int32]
+    L.bes_write_host.argtypes = [ctypes.POINTER(MeshArrays), ctypes.POINTER(Options), D,
+                                 ctypes.c_char_p, ctypes.c_int32, ctypes.c_char_p,
+                                 ctypes.c_size_t]
+    L.bes_solve.argtypes = [P, ctypes.POINTER(Output)]
     I64 = ctypes.POINTER(ctypes.c_int64)
     L.bes_host_geometry.argtypes = [ctypes.POINTER(MeshArrays), ctypes.c_int32, I64, I64, D, D, D,
                                     D, I64, I64, I64, I64, I64, I64, ctypes.c_char_p,
@@ -152,6 +171,36 @@ def options_from_besi(path: str) -> tuple[Options, str]:
     if rc != BES_OK:
         raise BesError(rc, err.value.decode())
     return o, mesh.value.decode()
+
+
+def default_output(**kw) -> Output:
+    """bes_output with the reference's defaults; keyword arguments override fields."""
+    o = Output()
+    load().bes_output_default(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v.encode() if k == "folder" else v)
+    return o
+
+
+def output_from_besi(path: str) -> Output:
+    o = Output()
+    err = ctypes.create_string_buffer(512)
+    rc = load().bes_output_from_besi(path.encode(), ctypes.byref(o), err, 512)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
+    return o
+
+
+def write_host(mesh, options: Options, U, path: str, kind: int = OUTPUT_VTK):
+    """bes_write_host: the reference's output file for state U [n_cells][5] (reference
+    numbering), on the host (no GPU)."""
+    keep = _MeshKeep(mesh)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    err = ctypes.create_string_buffer(512)
+    rc = load().bes_write_host(ctypes.byref(keep.c), ctypes.byref(options), _d(U),
+                               path.encode(), int(kind), err, 512)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
 
 
 def residual_norms_static(residual_ptr: int, n_cells: int, norms_ptr: int, stream: int = 0):
@@ -332,6 +381,14 @@ class Context:
         cnt = np.zeros(8, np.int64)
         self._check(load().bes_profile(self.h, int(enable), _d(ms), _i(cnt)))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.PROFILE_CATEGORIES)}
+
+    def write(self, path: str, kind: int = OUTPUT_VTK):
+        """bes_write: the reference's output file of the current state."""
+        self._check(load().bes_write(self.h, path.encode(), int(kind)))
+
+    def solve(self, output: Output | None = None):
+        """bes_solve: number_of_time_step steps with the reference's residual.csv and files."""
+        self._check(load().bes_solve(self.h, ctypes.byref(output or default_output())))
 
     def wall_force(self) -> np.ndarray:
         f = np.zeros(3)

@@ -203,8 +203,56 @@ int bes_counters(const bes_ctx* ctx, int64_t* out);
 /* Library build identification (e.g. "sm_103a"). */
 const char* bes_build_info(void);
 
+/* ---- Output files and the solve loop ------------------------------------------------
+ * The reference's writers, text for text (SolutionSnapshot::writePrimitiveToVtk / ToCsv /
+ * writeSlipWallToCsv, src/SolutionSnapshot.cpp:145-309): default std::ostream formatting
+ * (6 significant digits) of the "dimensional" primitives rho, Mach vector, gamma*p, gamma*R*T
+ * (GasPerfect_<T>::convertDimensional, src/GasPerfect.tpp:294-326). */
+#define BES_OUTPUT_VTK 0            /* solution as legacy ASCII VTK unstructured grid */
+#define BES_OUTPUT_CSV 1            /* solution as CSV: centroid, 6 primitives per cell */
+#define BES_OUTPUT_SLIP_WALL_CSV 2  /* slip-wall faces: centre, dimensional normal, owner's
+                                       6 primitives (zeroth-order surface values) */
+
+/* The .besi output keys (src/Config.cpp:155-187, 269-272). */
+typedef struct {
+  char folder[1024];      /* OUTPUT_FOLDER (default ".") */
+  int32_t format;         /* OUTPUT_FORMAT: BES_OUTPUT_VTK (default) or BES_OUTPUT_CSV */
+  int32_t slip_wall;      /* OUTPUT_SLIP_WALL: 1 YES, 0 NO (default) */
+  int64_t save_interval;  /* SAVE_INTERVAL: files after step k when k % SAVE_INTERVAL == 0
+                             and after the last step; 0 (default): after the last step only
+                             (the reference leaves it unset and divides by it) */
+  int32_t verbose;        /* 1: print the reference's console table to stdout */
+  int32_t reserved;
+} bes_output;
+
+void bes_output_default(bes_output* out);
+
+/* The output keys of a .besi file (other keys are left to bes_options_from_besi).  Same
+ * token rules as Config::readConfigFile_; a bad OUTPUT_FORMAT / OUTPUT_SLIP_WALL value ->
+ * BES_ERR_CONFIG. */
+int bes_output_from_besi(const char* besi_path, bes_output* out, char* err, size_t err_cap);
+
+/* Write the context's current state to `path` (kind BES_OUTPUT_*).  The VTK title line is
+ * `path`, as in the reference, which passes its own file name. */
+int bes_write(bes_ctx* ctx, const char* path, int32_t kind);
+
+/* Host-only (no GPU) form of bes_write for a state U [n_cells][5] in reference numbering;
+ * builds the reference-semantics mesh from `mesh` (gas constants and the MUSCL option from
+ * `opt`). */
+int bes_write_host(const bes_mesh_arrays* mesh, const bes_options* opt, const double* U,
+                   const char* path, int32_t kind, char* err, size_t err_cap);
+
+/* Solver::solve (src/SolverExplicit.cpp:395-438, src/SolverImplicit.cpp:552-600):
+ * NUMBER_OF_TIME_STEP steps of the context's solver from its current state.  residual.csv in
+ * out->folder is truncated, then every step appends "<step>," and the line the reference's
+ * timeStep_ logs (explicit: max |R| per variable of the last stage; implicit: max |RHS| per
+ * variable, linear iterations, linear error; "%e," formatting); solution_<step>.vtk|csv and
+ * (OUTPUT_SLIP_WALL) slip_wall_<step>.csv are written after the steps save_interval selects. */
+int bes_solve(bes_ctx* ctx, const bes_output* out);
+
 /* Sizes of the ABI structs as compiled: out[0] = sizeof(bes_options),
- * out[1] = sizeof(bes_mesh_arrays).  Lets a binding check its struct mirrors. */
+ * out[1] = sizeof(bes_mesh_arrays), out[2] = sizeof(bes_output).  out [3].  Lets a binding
+ * check its struct mirrors. */
 void bes_abi_sizes(int64_t* out);
 
 /* Host-only (no GPU): the mesh part of bes_create — face discovery, geometry and renumbering —

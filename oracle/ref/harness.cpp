@@ -2,7 +2,7 @@
 // TEST INFRASTRUCTURE ONLY: it runs the reference's own objects and dumps FP64 binary data
 // that pins the CPU restatement in oracle/ (the reference's ASCII outputs carry ~6 digits).
 //
-//   bes_ref_harness <case.besi> <outdir> <n_steps> [explicit|implicit|kat] [dump_ops]
+//   bes_ref_harness <case.besi> <outdir> <n_steps> [explicit|implicit|kat] [dump_ops] [write]
 //
 // It builds Config, Mesh, Gas and the solver exactly as main() does (src/BES.cpp:86-108),
 // sets the freestream initial condition, then calls the solver's own timeStep_ n_steps
@@ -12,7 +12,8 @@
 // plus the linear-solver iterations/error and the CFL.  With dump_ops it also writes, for
 // the initial state, the geometry, the time steps, Green-Gauss gradients, Venkatakrishnan
 // limiters, per-face MUSCL states and fluxes, first-order flux Jacobians and (implicit) the
-// assembled matrix and right-hand side.
+// assembled matrix and right-hand side.  With write it finally calls the reference's
+// Solver::writeToFile_ (solution file in OUTPUT_FORMAT, slip-wall CSV when OUTPUT_SLIP_WALL).
 #include "fluxroe_return_fix.hpp"
 
 #include <cmath>
@@ -165,7 +166,11 @@ int main(int argc, char** argv) {
   const std::string besi = argv[1];
   g_out = argv[2];
   const unsigned long nsteps = std::strtoul(argv[3], nullptr, 10);
-  const bool dump_ops = (argc > 5 && std::string(argv[5]) == "dump_ops");
+  bool dump_ops = false, write_out = false;
+  for (int a = 5; a < argc; ++a) {
+    dump_ops |= std::string(argv[a]) == "dump_ops";
+    write_out |= std::string(argv[a]) == "write";
+  }
 
   Config* config = new Config();
   Mesh* mesh = new Mesh();
@@ -285,6 +290,9 @@ int main(int argc, char** argv) {
       }
     }
     write_vec("residual_history.bin", hist);
+    // the reference's own writers, called as its solve loop does after the last step
+    // (src/SolverExplicit.cpp:427-433): solution_<n>.vtk|csv and slip_wall_<n>.csv
+    if (write_out) solver->writeToFile_(nsteps - 1, config->getNumCurrentSolution() - 1);
     SolutionSnapshot* s = solver->solution()->getCurrentSnapshot(nsteps, 0);
     std::vector<double> U(nc * 5);
     for (unsigned long i = 0; i < nc; ++i)
@@ -320,6 +328,7 @@ int main(int argc, char** argv) {
       }
     }
     write_vec("implicit_history.bin", hist);
+    if (write_out) solver->writeToFile_(nsteps - 1, config->getNumCurrentSolution() - 1);
     SolutionSnapshot* s = solver->solution_->getCurrentSnapshot(nsteps, 0);
     std::vector<double> U(nc * 5);
     for (unsigned long i = 0; i < nc; ++i)

@@ -58,6 +58,25 @@ CASES = {
                            12, "implicit", True),
 }
 
+# the reference's own output files (Solver::writeToFile_ after the last step, and the residual
+# lines its timeStep_ appends): name -> (mesh builder, options, steps, mode)
+OUTPUT_CASES = {
+    "output_explicit_vtk": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+                            dict(solver="EXPLICIT", local="YES", cfl=0.8, mach=(0.7, 0.05, 0),
+                                 out_format="VTK", out_slip="YES"),
+                            6, "explicit"),
+    "output_explicit_csv": (lambda: meshgen.gaussian_box(8, 4, 8),
+                            dict(solver="EXPLICIT", local="YES", cfl=0.8,
+                                 mach=meshgen.freestream_mach_vector(0.6, 2.0, -1.0),
+                                 out_format="CSV", out_slip="NO"),
+                            4, "explicit"),
+    "output_implicit_vtk": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+                            dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
+                                 mach=(0.84, 0, 0), smoother="ILU0", lin_tol=1e-2,
+                                 lin_maxiter=300, out_format="VTK", out_slip="YES"),
+                            4, "implicit"),
+}
+
 KAT_MACHS = {"kat_subsonic": (0.5, 0.1, -0.05), "kat_supersonic": (2.0, 0.2, 0.1)}
 
 
@@ -73,6 +92,8 @@ def besi_text(mesh_path: str, out_dir: str, o: dict, steps: int) -> str:
         "SAVE_INTERVAL = 100000",
         "FREESTREAM_MACH = " + ", ".join(repr(float(x)) for x in o["mach"]),
     ]
+    if o.get("out_format"):
+        lines += [f"OUTPUT_FORMAT = {o['out_format']}", f"OUTPUT_SLIP_WALL = {o['out_slip']}"]
     if o.get("fs_ramp"):
         lines += [f"FREESTREAM_RAMP = {o['fs_ramp']}",
                   f"FREESTREAM_RAMP_START_FRAC = {o['fs_frac']!r}"]
@@ -125,6 +146,33 @@ def run_case(name, builder, opts, steps, mode, dump):
     print(f"{name}: {mesh.n_cells} cells, {len(out)} arrays")
 
 
+def run_output_case(name, builder, opts, steps, mode):
+    """Fixture of the reference's output files; the output folder in the VTK title line is
+    replaced by {OUT}."""
+    mesh = builder()
+    with tempfile.TemporaryDirectory() as tmp:
+        msh = os.path.join(tmp, "mesh.msh")
+        meshgen.write_gmsh(mesh, msh)
+        besi = os.path.join(tmp, "case.besi")
+        with open(besi, "w") as f:
+            f.write(besi_text(msh, tmp, opts, steps))
+        subprocess.run([HARNESS, besi, tmp, str(steps), mode, "write"], check=True,
+                       env=dict(os.environ, OMP_NUM_THREADS="1"), stdout=subprocess.DEVNULL)
+        out = {"n_cells": mesh.n_cells, "final_state": _load(tmp, "final_state.bin")}
+        ext = opts["out_format"].lower()
+        files = {"solution": f"solution_{steps}.{ext}", "residual": "ref_residual.csv"}
+        if opts["out_slip"] == "YES":
+            files["slip_wall"] = f"slip_wall_{steps}.csv"
+        for key, fn in files.items():
+            with open(os.path.join(tmp, fn)) as f:
+                out[key] = np.array(f.read().replace(tmp, "{OUT}"))
+    meta = dict(opts)
+    meta["mach"] = list(map(float, opts["mach"]))
+    out["meta"] = np.array(repr(dict(meta=meta, steps=steps, mode=mode, mesh=mesh.name)))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(f"{name}: {mesh.n_cells} cells, files {sorted(files)}")
+
+
 def run_kat(name, mach, n=96, seed=7):
     rng = np.random.default_rng(seed)
     rho = rng.uniform(0.5, 2.0, (n, 2))
@@ -167,6 +215,10 @@ def main():
         if a.only and a.only != name:
             continue
         run_case(name, b, o, s, m, d)
+    for name, (b, o, s, m) in OUTPUT_CASES.items():
+        if a.only and a.only != name:
+            continue
+        run_output_case(name, b, o, s, m)
     for name, mach in KAT_MACHS.items():
         if a.only and a.only != name:
             continue

@@ -42,10 +42,11 @@ def test_exports_every_declared_symbol(native):
 
 def test_struct_mirrors_match(native):
     import ctypes
-    out = (ctypes.c_int64 * 2)()
+    out = (ctypes.c_int64 * 3)()
     native.bes_abi_sizes(out)
     assert out[0] == ctypes.sizeof(lib.Options)
     assert out[1] == ctypes.sizeof(lib.MeshArrays)
+    assert out[2] == ctypes.sizeof(lib.Output)
 
 
 def test_build_info_names_sm103a(native):
