@@ -272,6 +272,7 @@ void bes_destroy(bes_ctx* ctx) {
       if (ctx->kev[k][q]) cudaEventDestroy(ctx->kev[k][q]);
   if (ctx->imp.factor_graph) cudaGraphExecDestroy(ctx->imp.factor_graph);
   if (ctx->imp.apply_graph) cudaGraphExecDestroy(ctx->imp.apply_graph);
+  for (cudaGraphExec_t g : ctx->imp.colour_graphs) cudaGraphExecDestroy(g);
   for (cudaEvent_t e : ctx->prof.pool) cudaEventDestroy(e);
   for (void* p : ctx->allocations) cudaFree(p);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

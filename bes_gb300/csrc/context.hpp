@@ -71,7 +71,8 @@ struct ImplicitBuffers {
   void* X = nullptr;     // solution dW [5 nc]
   double* rhs = nullptr;       // FP64 right-hand side [5][nc]
   double* red = nullptr;       // reduction partials [64][kRedBlocks]
-  double* red_out = nullptr;   // reduced values [64]
+  double* red_out = nullptr;   // reduced values [128]
+  float* red_out_f = nullptr;  // FP32 copies of Gram-Schmidt coefficients [128]
   double* coef = nullptr;      // small coefficient vectors [64]
   int8_t* m_own = nullptr;     // per face local index in owner / neighbour
   int8_t* m_nb = nullptr;
@@ -79,6 +80,8 @@ struct ImplicitBuffers {
   int32_t* ilu_pos = nullptr;     // factorisation position of each cell
   cudaGraphExec_t factor_graph = nullptr;  // ILU factorisation, all stages
   cudaGraphExec_t apply_graph = nullptr;   // ILU forward+backward sweep, in place on Z
+  bool use_colour_ranges = false;          // colour order on contiguous colour ranges
+  std::vector<cudaGraphExec_t> colour_graphs;  // sweeps from V_0..V_m, then from W, into Z
   double cfl_actual = 0;
   double maxres[5] = {0, 0, 0, 0, 0};
   double maxres_old[5] = {0, 0, 0, 0, 0};

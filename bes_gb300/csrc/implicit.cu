@@ -117,18 +117,67 @@ void enqueue_ilu_factor(const Sys<T>& S) {
   }
 }
 
+// Colour-range sweeps (ilu_colour_kernel) from `in` into S.Z: colours 1..C-2 forward, the last
+// colour's two solves fused, colours C-2..0 backward.
+template <class T>
+void enqueue_ilu_colour_sweeps(const Sys<T>& S, const T* in) {
+  bes_ctx* c = S.c;
+  const SoaMesh& M = c->soa;
+  const int C = M.n_stages;
+  const int s1 = M.stage_off[1];
+  auto range = [&](int k, int& r0, int& r1) { r0 = M.stage_off[k]; r1 = M.stage_off[k + 1]; };
+  int r0, r1;
+  for (int k = 1; k < C - 1; ++k) {
+    range(k, r0, r1);
+    ilu_colour_kernel<T, true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
+        c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
+  }
+  range(C - 1, r0, r1);
+  ilu_colour_kernel<T, true, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(c->dm, r0, r1, s1, S.LU,
+                                                                       S.Dinv, in, S.Z);
+  for (int k = C - 2; k >= 0; --k) {
+    range(k, r0, r1);
+    ilu_colour_kernel<T, false, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
+        c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
+  }
+}
+
+// True when the factorisation order is the identity and every stage is a contiguous range of
+// cells in increasing order (colour order on the colour-major numbering).
+inline bool colour_ranges(const SoaMesh& M) {
+  if (M.n_stages < 1) return false;
+  for (int64_t i = 0; i < (int64_t)M.ilu_pos.size(); ++i)
+    if (M.ilu_pos[i] != i || M.stage_rows[i] != i) return false;
+  return true;
+}
+
 // Capture the stage-by-stage ILU work once per context as CUDA graphs (hundreds of small
-// kernels under level scheduling).
+// kernels under level scheduling).  With colour ranges there is one sweep graph per input
+// vector (the Krylov vectors V_0..V_m and W), so that no copy of the input is needed.
 template <class T>
 int ensure_ilu_graphs(const Sys<T>& S) {
   bes_ctx* c = S.c;
-  if (c->imp.apply_graph) return BES_OK;
+  if (c->imp.apply_graph || !c->imp.colour_graphs.empty()) return BES_OK;
   cudaGraph_t g;
   IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
   enqueue_ilu_factor(S);
   IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
   IMP_TRY(c, cudaGraphInstantiate(&c->imp.factor_graph, g, 0));
   cudaGraphDestroy(g);
+  if (c->imp.use_colour_ranges) {
+    const int nin = c->opt.gmres_restart + 2;  // V_0..V_m, then W
+    for (int q = 0; q < nin; ++q) {
+      const T* in = q + 1 < nin ? S.Vk(q) : S.W;
+      IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
+      enqueue_ilu_colour_sweeps(S, in);
+      IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
+      cudaGraphExec_t ge = nullptr;
+      IMP_TRY(c, cudaGraphInstantiate(&ge, g, 0));
+      cudaGraphDestroy(g);
+      c->imp.colour_graphs.push_back(ge);
+    }
+    return BES_OK;
+  }
   IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
   enqueue_ilu_sweeps(S);
   IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
@@ -141,7 +190,12 @@ int ensure_ilu_graphs(const Sys<T>& S) {
 template <class T>
 void precond_apply(const Sys<T>& S, const T* in, T* out) {
   bes_ctx* c = S.c;
-  if (uses_ilu(c)) {
+  if (uses_ilu(c) && c->imp.use_colour_ranges) {
+    // out is S.Z; in is one of V_0..V_m (graph q = its index) or W (the last graph)
+    const int64_t q = in == S.W ? (int64_t)c->imp.colour_graphs.size() - 1 : (in - S.V) / S.ldv;
+    cudaGraphLaunch(c->imp.colour_graphs[q], S.s);
+    c->launches += 2 * c->soa.n_stages - 1;
+  } else if (uses_ilu(c)) {
     if (in != out)
       cudaMemcpyAsync(out, in, (size_t)S.N * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
     cudaGraphLaunch(c->imp.apply_graph, S.s);
@@ -262,12 +316,13 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       prof_begin(c, PROF_ORTHO);
       launch_gs_dots<T>(nv, G, S.s, S.V, S.ldv, S.W, S.N, red);
       reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev);
-      gs_decide_kernel<<<1, 32, 0, S.s>>>(dev, nv, 1);
-      launch_gs_update<T, GS_FINAL1>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, S.N, red);
-      launch_gs_update<T, GS_REORTH>(nv, G, S.s, nullptr, S.W, S.V, S.ldv, dev, S.N, red);
+      float* devf = c->imp.red_out_f;
+      gs_decide_kernel<<<1, 64, 0, S.s>>>(dev, devf, nv, 1);
+      launch_gs_update<T, GS_FINAL1>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, devf, S.N, red);
+      launch_gs_update<T, GS_REORTH>(nv, G, S.s, nullptr, S.W, S.V, S.ldv, dev, devf, S.N, red);
       reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev + kGsH2);
-      gs_decide_kernel<<<1, 32, 0, S.s>>>(dev, nv, 2);
-      launch_gs_update<T, GS_FINAL2>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, S.N, red);
+      gs_decide_kernel<<<1, 64, 0, S.s>>>(dev, devf, nv, 2);
+      launch_gs_update<T, GS_FINAL2>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, devf, S.N, red);
       prof_end(c, PROF_ORTHO);
       S.c->launches += 8;
       double hbuf[kGsScalars];
@@ -444,6 +499,7 @@ int implicit_allocate(bes_ctx* c) {
     return BES_ERR_UNSUPPORTED;
   }
   if (o.linear_solver == 2) build_ilu_schedule(c->soa, true);
+  I.use_colour_ranges = o.linear_solver == 1 && colour_ranges(c->soa);
   if (uses_ilu(c)) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
   rc |= imp_malloc(c, &I.b, N * I.tsize);
@@ -454,6 +510,7 @@ int implicit_allocate(bes_ctx* c) {
   rc |= imp_malloc(c, (void**)&I.rhs, N * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.red, 64 * (size_t)std::max<int64_t>(kRedBlocks, nblk(nc, 128)) * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.red_out, 128 * sizeof(double));
+  rc |= imp_malloc(c, (void**)&I.red_out_f, 128 * sizeof(float));
   rc |= imp_malloc(c, (void**)&I.coef, 64 * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.m_own, nf);
   rc |= imp_malloc(c, (void**)&I.m_nb, nf);

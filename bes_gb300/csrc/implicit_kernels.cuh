@@ -387,6 +387,57 @@ __global__ void __launch_bounds__(128) ilu_upper_kernel(DevMesh m, const int32_t
   }
 }
 
+// Colour-ordered block-ILU(0) sweep when the colours are contiguous cell ranges in increasing
+// order (the colour-major numbering): the rows of one colour are [r0, r1), lower neighbours
+// are j < r0 and upper neighbours k >= r1, so no row list or position lookup is needed.  The
+// lower solve of colour 0 is the identity, so its y values are read from `in` where they are
+// needed (lower neighbours in [0, s1), colour 0's own upper solve) instead of being copied.
+//   LOWER only        colours 1..C-2 of the forward sweep: out_i = in_i - sum L_ij y_j
+//   LOWER and UPPER   the last colour: both solves at once (it has no upper neighbours)
+//   UPPER only        colours C-2..0 of the backward sweep: out_i = inv(U_ii)(y_i - sum U_ik z_k)
+// `in` and `out` must not alias.
+template <class T, bool LOWER, bool UPPER>
+__global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int r1, int s1,
+                                                         const T* __restrict__ A,
+                                                         const T* __restrict__ Dinv,
+                                                         const T* __restrict__ in,
+                                                         T* __restrict__ out) {
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  const int nc = m.nc;
+  const T* own = (LOWER || r0 == 0) ? in : out;
+  T acc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)v * nc + i];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int j = m.adj[s * nc + i];
+    const bool lower = LOWER && j >= 0 && j < r0;
+    const bool upper = UPPER && j >= r1;
+    if (!lower && !upper) continue;
+    const T* src = (lower && j < s1) ? in : out;
+    T y[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) y[v] = src[(int64_t)v * nc + j];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[r] -= ellc(A, 1 + s, r * 5 + c, nc, i) * y[c];
+  }
+  if (UPPER) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      T x = T(0);
+#pragma unroll
+      for (int c = 0; c < 5; ++c) x += Dinv[(int64_t)(r * 5 + c) * nc + i] * acc[c];
+      out[(int64_t)r * nc + i] = x;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[(int64_t)v * nc + i] = acc[v];
+  }
+}
+
 // block-Jacobi application: out_i = Dinv_i in_i
 template <class T>
 __global__ void __launch_bounds__(256) jacobi_apply_kernel(int nc, const T* __restrict__ Dinv,
@@ -446,18 +497,26 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restric
 template <class T> struct AccType { typedef double type; };
 template <> struct AccType<float> { typedef float type; };
 
-// Block reduction of NV per-thread accumulators; partials[k*gridDim + blk] (FP64).
-template <int NV, class A>
-__device__ __forceinline__ void block_reduce_store(A (&acc_in)[NV], double* partials) {
-  double acc[NV];
+// Warp sum in the accumulation type (FP32 for the FP32 system: FP64 arithmetic, conversions
+// included, runs on the FP64 pipe, which is ~60x slower on this GPU).
+template <class A>
+__device__ __forceinline__ A warp_sum_t(A x) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) acc[k] = (double)acc_in[k];
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Block reduction of NV per-thread accumulators; partials[k*gridDim + blk] (FP64).  Lanes are
+// summed in the accumulation type; each warp's sum is widened to FP64 once and the block's
+// eight warp sums are added in FP64 in a fixed order.
+template <int NV, class A>
+__device__ __forceinline__ void block_reduce_store(A (&acc)[NV], double* partials) {
   __shared__ double sh[NV][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    const double s = warp_sum(acc[k]);
-    if (lane == 0) sh[k][wid] = s;
+    const A s = warp_sum_t<A>(acc[k]);
+    if (lane == 0) sh[k][wid] = (double)s;
   }
   __syncthreads();
   for (int k = threadIdx.x; k < NV; k += blockDim.x) {
@@ -483,8 +542,21 @@ __device__ __forceinline__ void block_reduce_store(A (&acc_in)[NV], double* part
 //   dev[0..nv-1] h, dev[nv] |w|^2; dev[kGsH2 + k] h2, dev[kGsH2 + nv] |w'|^2;
 //   dev[kGsFlag] 1 if the second pass runs, dev[kGsInv] 1/h_{j+1,j} (0: leave V_{j+1}),
 //   dev[kGsNorm] h_{j+1,j}.
+//   devf: FP32 copies of h, h2, the flag and 1/h_{j+1,j} at the same offsets, written by
+//   gs_decide_kernel, so that FP32 update kernels convert nothing per thread.
 constexpr double kReorthTheta2 = 1.0 / 16.0;
 constexpr int kGsH2 = 40, kGsFlag = 80, kGsInv = 81, kGsNorm = 82, kGsScalars = 83;
+
+template <class A>
+__device__ __forceinline__ const A* gs_coef(const double* dev, const float* devf);
+template <>
+__device__ __forceinline__ const double* gs_coef<double>(const double* dev, const float*) {
+  return dev;
+}
+template <>
+__device__ __forceinline__ const float* gs_coef<float>(const double*, const float* devf) {
+  return devf;
+}
 
 // 16-byte unit of the vector kernels; the Krylov basis stride is a multiple of it
 template <class T>
@@ -529,8 +601,14 @@ __global__ void __launch_bounds__(256) gs_dots_kernel(const T* __restrict__ V, i
 
 // Decide after a reduction: stage 1 (after pass 1) sets the second-pass flag and, without a
 // second pass, 1/h_{j+1,j}; stage 2 (after pass 2) sets 1/h_{j+1,j} from the second pass.
-static __global__ void gs_decide_kernel(double* __restrict__ dev, int nv, int stage) {
-  if (threadIdx.x != 0) return;
+static __global__ void gs_decide_kernel(double* __restrict__ dev, float* __restrict__ devf,
+                                        int nv, int stage) {
+  if (threadIdx.x != 0) {
+    // FP32 copies of the coefficients this stage produced (threads 1..)
+    const int base = stage == 1 ? 0 : kGsH2;
+    for (int k = threadIdx.x - 1; k < nv; k += blockDim.x - 1) devf[base + k] = (float)dev[base + k];
+    return;
+  }
   if (stage == 1) {
     const double nw2 = dev[nv];
     double s = 0.0;
@@ -541,6 +619,8 @@ static __global__ void gs_decide_kernel(double* __restrict__ dev, int nv, int st
     const double hn = reorth ? 0.0 : sqrt(est);
     dev[kGsNorm] = hn;
     dev[kGsInv] = hn > 0.0 ? 1.0 / hn : 0.0;
+    devf[kGsFlag] = reorth ? 1.0f : 0.0f;
+    devf[kGsInv] = (float)dev[kGsInv];
   } else {
     if (dev[kGsFlag] == 0.0) return;
     const double nw2 = dev[kGsH2 + nv];
@@ -550,6 +630,7 @@ static __global__ void gs_decide_kernel(double* __restrict__ dev, int nv, int st
     const double hn = e2 > 0.0 ? sqrt(e2) : 0.0;
     dev[kGsNorm] = hn;
     dev[kGsInv] = hn > 0.0 ? 1.0 / hn : 0.0;
+    devf[kGsInv] = (float)dev[kGsInv];
   }
 }
 
@@ -562,20 +643,21 @@ template <class T, int NV, int MODE>
 __global__ void __launch_bounds__(256) gs_update_kernel(T* __restrict__ out, T* w,
                                                         const T* __restrict__ V, int64_t ldv,
                                                         const double* __restrict__ dev,
+                                                        const float* __restrict__ devf,
                                                         int64_t N, double* __restrict__ partials) {
   typedef typename AccType<T>::type A;
   typedef Pack16<T> P;
   constexpr int W = P::W;
-  const bool second = dev[kGsFlag] != 0.0;
+  const A* cf = gs_coef<A>(dev, devf);
+  const bool second = cf[kGsFlag] != A(0);
   const bool runs = MODE == GS_FINAL1 ? !second : second;
   if (!runs) return;
-  const double* coef = MODE == GS_FINAL2 ? dev + kGsH2 : dev;
-  const double invd = dev[kGsInv];
-  if (MODE != GS_REORTH && invd == 0.0) return;  // h_{j+1,j} = 0: V_{j+1} is not used
-  const A inv = (A)invd;
+  const A* coef = MODE == GS_FINAL2 ? cf + kGsH2 : cf;
+  const A inv = cf[kGsInv];
+  if (MODE != GS_REORTH && inv == A(0)) return;  // h_{j+1,j} = 0: V_{j+1} is not used
   A c[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) c[k] = (A)coef[k];
+  for (int k = 0; k < NV; ++k) c[k] = coef[k];
   constexpr int NA = MODE == GS_REORTH ? NV + 1 : 1;
   A acc[NA];
 #pragma unroll
@@ -652,10 +734,10 @@ void launch_gs_dots(int nvec, int G, cudaStream_t s, const T* V, int64_t ldv, co
 
 template <class T, int MODE>
 void launch_gs_update(int nvec, int G, cudaStream_t s, T* out, T* w, const T* V, int64_t ldv,
-                      const double* dev, int64_t N, double* partials) {
+                      const double* dev, const float* devf, int64_t N, double* partials) {
   switch (nvec) {
 #define BES_UPD_CASE(n) \
-  case n: gs_update_kernel<T, n, MODE><<<G, 256, 0, s>>>(out, w, V, ldv, dev, N, partials); break;
+  case n: gs_update_kernel<T, n, MODE><<<G, 256, 0, s>>>(out, w, V, ldv, dev, devf, N, partials); break;
     BES_NV_CASES(BES_UPD_CASE)
 #undef BES_UPD_CASE
     default: break;
@@ -708,7 +790,7 @@ __global__ void __launch_bounds__(256) norm2_kernel(const T* __restrict__ x, int
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x)
     sa += (A)x[idx] * (A)x[idx];
-  double s = warp_sum((double)sa);
+  const double s = (double)warp_sum_t<A>(sa);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x < 32) {
