@@ -74,39 +74,43 @@ void enqueue_iteration(bes_ctx* ctx, int cur) {
   const bes_options& o = ctx->opt;
   const DevMesh& m = ctx->dm;
   const int nb_c = blocks_for(m.nc), nb_f = blocks_for(m.nf);
+  const dim3 gc(nb_c, ctx->nb), gf(nb_f, ctx->nb);  // y: condition
   double* Un = ctx->U[cur];
   double* Uk = ctx->U[cur ^ 1];
   const int local = o.local_time_step;
   cudaStream_t s = ctx->stream;
-  freestream_step_kernel<<<1, 1, 0, s>>>(ctx->prm, ctx->step_dev, ctx->pinf_dev, ctx->dtmin);
+  freestream_step_kernel<<<1, 128, 0, s>>>(ctx->prm, ctx->nb, ctx->step_dev, ctx->pinf_dev,
+                                           ctx->dtmin, ctx->iter_ctr, ctx->iter_cur);
   for (int k = 0; k < o.n_stage; ++k) {
     cudaEvent_t* e = ctx->kev[k];
     const double* Uin = (k == 0) ? Un : Uk;
     cudaEventRecordWithFlags(e[0], s, cudaEventRecordExternal);
     if (k == 0)
-      cell_recon_kernel<true, false><<<nb_c, kBlock, 0, s>>>(
+      cell_recon_kernel<true, false><<<gc, kBlock, 0, s>>>(
           m, ctx->prm, Uin, ctx->RS, ctx->rs_ld, ctx->dt, o.courant_num, local, ctx->dtmin,
           nullptr, nullptr);
     else
-      cell_recon_kernel<false, false><<<nb_c, kBlock, 0, s>>>(
+      cell_recon_kernel<false, false><<<gc, kBlock, 0, s>>>(
           m, ctx->prm, Uin, ctx->RS, ctx->rs_ld, ctx->dt, o.courant_num, local, ctx->dtmin,
           nullptr, nullptr);
     cudaEventRecordWithFlags(e[1], s, cudaEventRecordExternal);
     cudaEventRecordWithFlags(e[2], s, cudaEventRecordExternal);
-    face_flux_kernel<false><<<nb_f, kBlock, 0, s>>>(m, ctx->prm, ctx->RS, ctx->rs_ld, ctx->FA,
-                                                    nullptr, ctx->nan_flag);
+    face_flux_kernel<false><<<gf, kBlock, 0, s>>>(m, ctx->prm, ctx->RS, ctx->rs_ld, ctx->FA,
+                                                  nullptr, ctx->nan_flag);
     cudaEventRecordWithFlags(e[3], s, cudaEventRecordExternal);
     cudaEventRecordWithFlags(e[4], s, cudaEventRecordExternal);
     if (k == o.n_stage - 1)
-      update_kernel<true><<<nb_c, kBlock, 0, s>>>(m, ctx->FA, Un, Uk, ctx->dt, ctx->dtmin, local,
-                                                  o.stage_coeff[k], ctx->partials, nullptr);
+      update_kernel<true><<<gc, kBlock, 0, s>>>(m, ctx->FA, Un, Uk, ctx->dt, ctx->dtmin, local,
+                                                o.stage_coeff[k], ctx->partials, nullptr,
+                                                ctx->prm.active);
     else
-      update_kernel<false><<<nb_c, kBlock, 0, s>>>(m, ctx->FA, Un, Uk, ctx->dt, ctx->dtmin, local,
-                                                   o.stage_coeff[k], ctx->partials, nullptr);
+      update_kernel<false><<<gc, kBlock, 0, s>>>(m, ctx->FA, Un, Uk, ctx->dt, ctx->dtmin, local,
+                                                 o.stage_coeff[k], ctx->partials, nullptr,
+                                                 ctx->prm.active);
     cudaEventRecordWithFlags(e[5], s, cudaEventRecordExternal);
   }
-  finalize_norms_kernel<<<1, kBlock, 0, s>>>(ctx->partials, nb_c, ctx->hist, ctx->hist_cap,
-                                             ctx->iter_ctr);
+  finalize_norms_kernel<<<ctx->nb, kBlock, 0, s>>>(ctx->partials, nb_c, ctx->hist, ctx->hist_cap,
+                                                   ctx->iter_cur);
 }
 
 int build_graphs(bes_ctx* ctx) {
@@ -123,14 +127,19 @@ int build_graphs(bes_ctx* ctx) {
   return BES_OK;
 }
 
+// [nb][nc][5] in reference numbering -> [nb][5][nc] in the device numbering
 void fill_state_aos_to_soa(const bes_ctx* ctx, const double* U, std::vector<double>& soa) {
   const int64_t nc = ctx->soa.nc;
-  soa.resize(5 * nc);
-  for (int64_t i = 0; i < nc; ++i) {
-    const int64_t c = ctx->soa.cell_new2ref[i];
-    for (int v = 0; v < 5; ++v) soa[v * nc + i] = U[c * 5 + v];
-  }
+  soa.resize(5 * nc * ctx->nb);
+  for (int64_t b = 0; b < ctx->nb; ++b)
+    for (int64_t i = 0; i < nc; ++i) {
+      const int64_t c = ctx->soa.cell_new2ref[i];
+      for (int v = 0; v < 5; ++v) soa[(b * 5 + v) * nc + i] = U[(b * nc + c) * 5 + v];
+    }
 }
+
+int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_cond,
+                   const double* mach, bes_ctx** out);
 
 }  // namespace
 
@@ -171,12 +180,30 @@ void bes_options_default(bes_options* o) {
 }
 
 int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** out) {
+  if (!opt) return BES_ERR_INVALID;
+  return create_context(mesh, opt, 1, opt->freestream_mach, out);
+}
+
+int bes_create_batch(const bes_mesh_arrays* mesh, const bes_options* opt, int32_t n_cond,
+                     const double* mach, bes_ctx** out) {
+  if (!opt || !mach || n_cond < 1) return BES_ERR_INVALID;
+  if (opt->solver_type != 0 && n_cond > 1) return BES_ERR_UNSUPPORTED;
+  return create_context(mesh, opt, n_cond, mach, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_cond,
+                   const double* mach, bes_ctx** out) {
   if (!mesh || !opt || !out) return BES_ERR_INVALID;
   *out = nullptr;
   if (opt->n_stage < 1 || opt->n_stage > 8) return BES_ERR_INVALID;
   std::unique_ptr<bes_ctx> ctx(new (std::nothrow) bes_ctx());
   if (!ctx) return BES_ERR_INVALID;
   ctx->opt = *opt;
+  ctx->nb = n_cond;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     *out = nullptr;
@@ -222,32 +249,47 @@ int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** ou
   rc |= upload(c, &m.fn, S.fn);
   rc |= upload(c, &m.farea, S.farea);
   if (rc) return BES_ERR_CUDA;
-  const int64_t nc = S.nc, nf = S.nf;
+  const int64_t nc = S.nc, nf = S.nf, nb = n_cond;
   c->rs_ld = nc * S.nslots + S.n_extra;
-  rc |= dev_alloc(c, &c->U[0], 5 * nc);
-  rc |= dev_alloc(c, &c->U[1], 5 * nc);
-  rc |= dev_alloc(c, &c->RS, 5 * c->rs_ld);
-  rc |= dev_alloc(c, &c->FA, 5 * nf);
-  rc |= dev_alloc(c, &c->dt, nc);
+  rc |= dev_alloc(c, &c->U[0], 5 * nc * nb);
+  rc |= dev_alloc(c, &c->U[1], 5 * nc * nb);
+  rc |= dev_alloc(c, &c->RS, 5 * c->rs_ld * nb);
+  rc |= dev_alloc(c, &c->FA, 5 * nf * nb);
+  rc |= dev_alloc(c, &c->dt, nc * nb);
   c->max_blocks = blocks_for(nc);
-  rc |= dev_alloc(c, &c->partials, 10 * (size_t)c->max_blocks);
-  rc |= dev_alloc(c, &c->dtmin, 1);
-  c->hist_cap = 4096;
-  rc |= dev_alloc(c, &c->hist, 10 * c->hist_cap);
+  rc |= dev_alloc(c, &c->partials, 10 * (size_t)c->max_blocks * nb);
+  rc |= dev_alloc(c, &c->dtmin, nb);
+  c->hist_cap = std::max<int64_t>(16, 4096 / nb);  // iterations per history chunk
+  rc |= dev_alloc(c, &c->hist, 10 * c->hist_cap * nb);
   rc |= dev_alloc(c, &c->iter_ctr, 1);
+  rc |= dev_alloc(c, &c->iter_cur, 1);
   rc |= dev_alloc(c, &c->nan_flag, 1);
-  rc |= dev_alloc(c, &c->pinf_dev, 6);
+  rc |= dev_alloc(c, &c->pinf_dev, 6 * nb);
+  rc |= dev_alloc(c, &c->pinf0_dev, 6 * nb);
+  rc |= dev_alloc(c, &c->active_dev, nb);
   rc |= dev_alloc(c, &c->step_dev, 1);
   if (rc) return BES_ERR_CUDA;
   BES_CUDA_TRY(c, cudaMemset(c->iter_ctr, 0, sizeof(int64_t)));
   BES_CUDA_TRY(c, cudaMemset(c->nan_flag, 0, sizeof(int)));
-  // gas and freestream (Config::initializePostMesh, src/Config.cpp:480-488)
+  // gas and freestream (Config::initializePostMesh, src/Config.cpp:480-488), per condition
   c->prm.gas = make_gas(opt->gas_constant, opt->specific_heat_ratio, opt->harten_correction_limit);
-  c->prm.pinf[0] = 1.0;
-  for (int d = 0; d < 3; ++d) c->prm.pinf[1 + d] = opt->freestream_mach[d];
-  c->prm.pinf[4] = 1.0 / opt->specific_heat_ratio;
-  c->prm.pinf[5] = 1.0 / (opt->specific_heat_ratio * opt->gas_constant);
+  c->pinf0_host.assign(6 * nb, 0.0);
+  for (int64_t b = 0; b < nb; ++b) {
+    double* p = &c->pinf0_host[6 * b];
+    p[0] = 1.0;
+    for (int d = 0; d < 3; ++d) p[1 + d] = mach[3 * b + d];
+    p[4] = 1.0 / opt->specific_heat_ratio;
+    p[5] = 1.0 / (opt->specific_heat_ratio * opt->gas_constant);
+  }
+  for (int i = 0; i < 6; ++i) c->prm.pinf[i] = c->pinf0_host[i];
+  BES_CUDA_TRY(c, cudaMemcpy(c->pinf0_dev, c->pinf0_host.data(), 6 * nb * sizeof(double),
+                             cudaMemcpyHostToDevice));
+  c->active_host.assign(nb, 1);
+  BES_CUDA_TRY(c, cudaMemcpy(c->active_dev, c->active_host.data(), nb * sizeof(int32_t),
+                             cudaMemcpyHostToDevice));
   c->prm.pinf_dev = c->pinf_dev;
+  c->prm.pinf0_dev = c->pinf0_dev;
+  c->prm.active = nb > 1 ? c->active_dev : nullptr;
   c->prm.ramp_steps = opt->freestream_ramp;
   c->prm.ramp_frac = opt->freestream_ramp_start_frac;
   rc = build_graphs(c);
@@ -261,6 +303,10 @@ int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** ou
   *out = ctx.release();
   return BES_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 void bes_destroy(bes_ctx* ctx) {
   if (!ctx) return;
@@ -298,21 +344,26 @@ int bes_set_freestream_state(bes_ctx* ctx) {
   const int64_t zero = 0;
   BES_CUDA_TRY(ctx, cudaMemcpy(ctx->step_dev, &zero, sizeof(zero), cudaMemcpyHostToDevice));
   // GasPerfect_::computeAllConservedVariable of the step-0 freestream primitives
-  // (:182-216; setUniversalInitialCondition gets getFreestreamPrimitiveVariables(0))
-  double P[6];
-  freestream_at(ctx->prm, 0, P);
-  BES_CUDA_TRY(ctx, cudaMemcpy(ctx->pinf_dev, P, sizeof(P), cudaMemcpyHostToDevice));
-  double Uf[5];
-  Uf[0] = P[0];
-  double s = 0;
-  for (int d = 0; d < 3; ++d) {
-    Uf[1 + d] = Uf[0] * P[1 + d];
-    s += P[1 + d] * P[1 + d];
+  // (:182-216; setUniversalInitialCondition gets getFreestreamPrimitiveVariables(0)), for
+  // every condition
+  const int64_t nc = ctx->soa.nc, nb = ctx->nb;
+  std::vector<double> soa(5 * nc * nb), P(6 * nb);
+  for (int64_t b = 0; b < nb; ++b) {
+    double* p = &P[6 * b];
+    freestream_from(&ctx->pinf0_host[6 * b], ctx->prm.ramp_steps, ctx->prm.ramp_frac, 0, p);
+    double Uf[5];
+    Uf[0] = p[0];
+    double s = 0;
+    for (int d = 0; d < 3; ++d) {
+      Uf[1 + d] = Uf[0] * p[1 + d];
+      s += p[1 + d] * p[1 + d];
+    }
+    Uf[4] = Uf[0] * (ctx->prm.gas.cv * p[5] + s / 2.0);
+    for (int v = 0; v < 5; ++v)
+      std::fill(soa.begin() + (b * 5 + v) * nc, soa.begin() + (b * 5 + v + 1) * nc, Uf[v]);
   }
-  Uf[4] = Uf[0] * (ctx->prm.gas.cv * P[5] + s / 2.0);
-  const int64_t nc = ctx->soa.nc;
-  std::vector<double> soa(5 * nc);
-  for (int v = 0; v < 5; ++v) std::fill(soa.begin() + v * nc, soa.begin() + (v + 1) * nc, Uf[v]);
+  BES_CUDA_TRY(ctx, cudaMemcpy(ctx->pinf_dev, P.data(), P.size() * sizeof(double),
+                               cudaMemcpyHostToDevice));
   ctx->cur = 0;
   BES_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->U[0], soa.data(), soa.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
   BES_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -330,14 +381,15 @@ int bes_set_state(bes_ctx* ctx, const double* U) {
 
 int bes_get_state(bes_ctx* ctx, double* U) {
   if (!ctx || !U) return BES_ERR_INVALID;
-  const int64_t nc = ctx->soa.nc;
-  std::vector<double> soa(5 * nc);
+  const int64_t nc = ctx->soa.nc, nb = ctx->nb;
+  std::vector<double> soa(5 * nc * nb);
   BES_CUDA_TRY(ctx, cudaMemcpyAsync(soa.data(), ctx->U[ctx->cur], soa.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
   BES_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  for (int64_t i = 0; i < nc; ++i) {
-    const int64_t c = ctx->soa.cell_new2ref[i];
-    for (int v = 0; v < 5; ++v) U[c * 5 + v] = soa[v * nc + i];
-  }
+  for (int64_t b = 0; b < nb; ++b)
+    for (int64_t i = 0; i < nc; ++i) {
+      const int64_t c = ctx->soa.cell_new2ref[i];
+      for (int v = 0; v < 5; ++v) U[(b * nc + c) * 5 + v] = soa[(b * 5 + v) * nc + i];
+    }
   return BES_OK;
 }
 
@@ -355,7 +407,8 @@ int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history) {
     int rc = bes_explicit_enqueue(ctx, chunk);
     if (rc) return rc;
     if (history)
-      BES_CUDA_TRY(ctx, cudaMemcpyAsync(history + done * 10, ctx->hist, chunk * 10 * sizeof(double),
+      BES_CUDA_TRY(ctx, cudaMemcpyAsync(history + done * 10 * ctx->nb, ctx->hist,
+                                        chunk * 10 * ctx->nb * sizeof(double),
                                         cudaMemcpyDeviceToHost, ctx->stream));
     rc = check_nan(ctx);  // synchronises the stream
     if (rc) return rc;
@@ -367,6 +420,10 @@ int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history) {
 int bes_compute_operators(bes_ctx* ctx, double cfl, double* dt, double* grad, double* limiter,
                           double* face_UL, double* face_UR, double* face_flux, double* residual) {
   if (!ctx) return BES_ERR_INVALID;
+  if (ctx->nb != 1) {
+    ctx->last_error = "operators are evaluated on single-condition contexts";
+    return BES_ERR_UNSUPPORTED;
+  }
   bes_ctx* c = ctx;
   const int64_t nc = c->soa.nc, nf = c->soa.nf;
   if (!c->G) {
@@ -492,22 +549,95 @@ int bes_wall_force(bes_ctx* ctx, double* force) {
   // Integrated slip-wall pressure force sum_f p_owner S_f with the owner cell's pressure, the
   // quantity of the reference's slip-wall output (SolutionSnapshot::writeSlipWallToCsv,
   // src/SolutionSnapshot.cpp:268-309), in non-dimensional units, summed in face order.
+  // Batched contexts: force [n_cond][3].
   const int64_t nc = ctx->soa.nc;
-  std::vector<double> U(5 * nc);
+  std::vector<double> U(5 * nc * ctx->nb);
   int rc = bes_get_state(ctx, U.data());
   if (rc) return rc;
   const RefMesh& R = ctx->ref;
   const double gm1 = ctx->prm.gas.gm1;
-  double F[3] = {0, 0, 0};
-  for (int64_t f = 0; f < R.nf; ++f) {
-    if (R.kind[f] != KIND_SLIP_WALL) continue;
-    const double* u = &U[R.owner[f] * 5];
-    const double k = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
-    const double p = gm1 * (u[4] - k / (2.0 * u[0]));
-    for (int d = 0; d < 3; ++d) F[d] += p * R.S[f * 3 + d];
+  for (int64_t b = 0; b < ctx->nb; ++b) {
+    double F[3] = {0, 0, 0};
+    for (int64_t f = 0; f < R.nf; ++f) {
+      if (R.kind[f] != KIND_SLIP_WALL) continue;
+      const double* u = &U[(b * nc + R.owner[f]) * 5];
+      const double k = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
+      const double p = gm1 * (u[4] - k / (2.0 * u[0]));
+      for (int d = 0; d < 3; ++d) F[d] += p * R.S[f * 3 + d];
+    }
+    for (int d = 0; d < 3; ++d) force[b * 3 + d] = F[d];
   }
-  for (int d = 0; d < 3; ++d) force[d] = F[d];
   return BES_OK;
+}
+
+int bes_conditions(const bes_ctx* ctx, int32_t* n_cond) {
+  if (!ctx || !n_cond) return BES_ERR_INVALID;
+  *n_cond = ctx->nb;
+  return BES_OK;
+}
+
+int bes_set_active(bes_ctx* ctx, const int32_t* active) {
+  if (!ctx || !active) return BES_ERR_INVALID;
+  for (int b = 0; b < ctx->nb; ++b) ctx->active_host[b] = active[b] ? 1 : 0;
+  BES_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->active_dev, ctx->active_host.data(),
+                                    ctx->nb * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  BES_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BES_OK;
+}
+
+int bes_sweep_run(bes_ctx* ctx, int64_t max_iter, double drop, int64_t check_every,
+                  int64_t* iters, double* final_drop) {
+  if (!ctx || max_iter < 0 || check_every < 1) return BES_ERR_INVALID;
+  if (ctx->opt.solver_type != 0) {
+    ctx->last_error = "bes_sweep_run drives the explicit solver";
+    return BES_ERR_UNSUPPORTED;
+  }
+  const int nb = ctx->nb;
+  std::vector<double> r0(nb, -1.0), last(nb, 0.0);
+  std::vector<int64_t> conv(nb, -1);
+  std::vector<int32_t> act(nb, 1);
+  int rc = bes_set_active(ctx, act.data());
+  if (rc) return rc;
+  std::vector<double> hist;
+  int64_t done = 0;
+  int n_active = nb;
+  while (done < max_iter && n_active > 0) {
+    const int64_t n = std::min<int64_t>(check_every, max_iter - done);
+    hist.assign((size_t)n * nb * 10, 0.0);
+    rc = bes_explicit_iterations(ctx, n, hist.data());
+    if (rc) return rc;
+    for (int64_t q = 0; q < n; ++q)
+      for (int b = 0; b < nb; ++b) {
+        if (!act[b] || conv[b] >= 0) continue;
+        const double* h = &hist[((size_t)q * nb + b) * 10];
+        double r = 0.0;
+        for (int v = 0; v < 5; ++v) r += h[v] * h[v];
+        r = std::sqrt(r);
+        if (r0[b] < 0) r0[b] = r;
+        last[b] = r0[b] > 0 ? r / r0[b] : 0.0;
+        if (!(r <= drop * r0[b]) && std::isfinite(r)) continue;
+        conv[b] = done + q + 1;  // converged (or diverged to a non-finite residual)
+      }
+    done += n;
+    bool changed = false;
+    for (int b = 0; b < nb; ++b)
+      if (act[b] && conv[b] >= 0) {
+        act[b] = 0;
+        --n_active;
+        changed = true;
+      }
+    if (changed && n_active > 0) {
+      rc = bes_set_active(ctx, act.data());
+      if (rc) return rc;
+    }
+  }
+  for (int b = 0; b < nb; ++b) {
+    if (iters) iters[b] = conv[b] >= 0 ? conv[b] : done;
+    if (final_drop) final_drop[b] = last[b];
+  }
+  std::fill(act.begin(), act.end(), 1);
+  return bes_set_active(ctx, act.data());
 }
 
 }  // extern "C"

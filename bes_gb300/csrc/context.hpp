@@ -28,19 +28,26 @@ struct DevMesh {
 struct Params {
   GasConst gas;
   double pinf[6];        // freestream primitives (rho, u, v, w, p, T), Config.cpp:480-488
-  const double* pinf_dev;  // the current step's freestream primitives (device, ramped)
+  const double* pinf_dev;  // the current step's freestream primitives (device, ramped),
+                           // [6] per condition
+  const double* pinf0_dev = nullptr;  // unramped freestream primitives, [6] per condition
+  const int32_t* active = nullptr;    // per condition: 0 = frozen (its state is kept)
   int32_t ramp_steps;      // FREESTREAM_RAMP
   double ramp_frac;        // FREESTREAM_RAMP_START_FRAC
 };
 
 // Freestream primitives of step t (Config::getFreestreamPrimitiveVariables,
 // src/Config.cpp:688-706): the velocity ramps from frac * u_inf to u_inf over ramp_steps.
-BES_HD void freestream_at(const Params& p, int64_t t, double* out) {
-  for (int i = 0; i < 6; ++i) out[i] = p.pinf[i];
-  if (p.ramp_steps > 0 && t < p.ramp_steps) {
-    const double s = p.ramp_frac + (double)t / (double)p.ramp_steps * (1 - p.ramp_frac);
-    for (int d = 0; d < 3; ++d) out[1 + d] = p.pinf[1 + d] * s;
+BES_HD void freestream_from(const double* base, int32_t ramp_steps, double ramp_frac, int64_t t,
+                            double* out) {
+  for (int i = 0; i < 6; ++i) out[i] = base[i];
+  if (ramp_steps > 0 && t < ramp_steps) {
+    const double s = ramp_frac + (double)t / (double)ramp_steps * (1 - ramp_frac);
+    for (int d = 0; d < 3; ++d) out[1 + d] = base[1 + d] * s;
   }
+}
+BES_HD void freestream_at(const Params& p, int64_t t, double* out) {
+  freestream_from(p.pinf, p.ramp_steps, p.ramp_frac, t, out);
 }
 
 template <class T>
@@ -138,6 +145,14 @@ struct bes_ctx {
   double* hist = nullptr;               // device history [hist_cap][10]
   int64_t hist_cap = 0;
   int64_t* iter_ctr = nullptr;
+  int64_t* iter_cur = nullptr;    // history row of the running iteration
+  // batched conditions (bes_create_batch): nb freestream conditions share the mesh; every
+  // per-condition array holds nb copies side by side ([condition][...])
+  int nb = 1;
+  double* pinf0_dev = nullptr;       // [nb][6]
+  int32_t* active_dev = nullptr;     // [nb]
+  std::vector<double> pinf0_host;    // [nb][6]
+  std::vector<int32_t> active_host;  // [nb]
   int* nan_flag = nullptr;  // face index + 1 of a NaN flux (0 none)
   double* pinf_dev = nullptr;     // [6] freestream primitives of the current step
   int64_t* step_dev = nullptr;    // solver step counter read by the explicit graphs

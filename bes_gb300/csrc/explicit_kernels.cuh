@@ -30,6 +30,14 @@ __device__ __forceinline__ double warp_min(double x) {
   return x;
 }
 
+// Batched conditions: blockIdx.y is the condition; its U, RS, FA, dt, dtmin, partials and
+// freestream follow the first condition's at fixed strides ([condition][...]).  A condition
+// whose Params::active entry is 0 is frozen: the sweeps skip it and the last update copies
+// its state forward.
+__device__ __forceinline__ bool condition_frozen(const Params& prm) {
+  return prm.active != nullptr && prm.active[blockIdx.y] == 0;
+}
+
 // Cell sweep.  U is [5][nc]; RS is [5][ldr] with ldr >= nc*nslots + n_extra.
 template <bool STAGE0, bool WRITE_GL>
 __global__ void __launch_bounds__(kBlock) cell_recon_kernel(
@@ -38,6 +46,14 @@ __global__ void __launch_bounds__(kBlock) cell_recon_kernel(
     double* __restrict__ G_out, double* __restrict__ phi_out) {
   const int nc = m.nc;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (condition_frozen(prm)) return;
+  {
+    const int64_t b = blockIdx.y;
+    U += b * 5 * nc;
+    RS += b * 5 * ldr;
+    dt += b * nc;
+    dtmin += b;
+  }
   double dt_c = 1e300;
   if (c < nc) {
     double u[5];
@@ -201,7 +217,11 @@ __global__ void __launch_bounds__(kBlock) face_flux_kernel(
     double* __restrict__ F_out, int* __restrict__ nan_flag) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   const int nf = m.nf;
-  if (f >= nf) return;
+  if (f >= nf || condition_frozen(prm)) return;
+  const int64_t b = blockIdx.y;
+  RS += b * 5 * ldr;
+  FA += b * 5 * nf;
+  const double* pinf = prm.pinf_dev + 6 * b;
   double UL[5], F[5];
   const int so = m.fsrc_own[f];
 #pragma unroll
@@ -218,7 +238,7 @@ __global__ void __launch_bounds__(kBlock) face_flux_kernel(
   } else if (f < m.nf_int + m.nf_slip) {
     slipwall_flux(prm.gas, UL, n, F);
   } else {
-    freestream_flux(prm.gas, UL, prm.pinf_dev, n, F);
+    freestream_flux(prm.gas, UL, pinf, n, F);
   }
   const double A = m.farea[f];
   bool bad = false;
@@ -236,11 +256,27 @@ __global__ void __launch_bounds__(kBlock) update_kernel(
     DevMesh m, const double* __restrict__ FA, const double* __restrict__ Un,
     double* __restrict__ Uout, const double* __restrict__ dt,
     const unsigned long long* __restrict__ dtmin, int local_dt, double alpha,
-    double* __restrict__ partials, double* __restrict__ R_out) {
+    double* __restrict__ partials, double* __restrict__ R_out, const int32_t* active = nullptr) {
   const int nc = m.nc, nf = m.nf;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  {
+    const int64_t b = blockIdx.y;
+    FA += b * 5 * nf;
+    Un += b * 5 * nc;
+    Uout += b * 5 * nc;
+    dt += b * nc;
+    dtmin += b;
+    partials += b * 10 * gridDim.x;
+  }
+  const bool frozen = active != nullptr && active[blockIdx.y] == 0;
+  if (frozen && !LAST) return;
   double R[5] = {0, 0, 0, 0, 0};
-  if (c < nc) {
+  if (frozen) {
+    // keep the state: the last stage's output becomes the next iteration's input
+    if (c < nc)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) Uout[(int64_t)v * nc + c] = Un[(int64_t)v * nc + c];
+  } else if (c < nc) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int g = m.gface[q * nc + c];
@@ -283,13 +319,16 @@ __global__ void __launch_bounds__(kBlock) update_kernel(
   }
 }
 
-// One block: reduce the per-block partials in a fixed order into history[iter] (L2, max).
+// One block per condition: reduce the per-block partials in a fixed order into
+// history[iter][condition] (L2, max); iter = *iter_cur (set by freestream_step_kernel).
 static __global__ void __launch_bounds__(kBlock) finalize_norms_kernel(
     const double* __restrict__ partials, int nblocks, double* __restrict__ hist,
-    int64_t hist_cap, int64_t* __restrict__ iter_ctr) {
+    int64_t hist_cap, const int64_t* __restrict__ iter_cur) {
   __shared__ double sh[kBlock / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t it = *iter_ctr;
+  const int64_t it = *iter_cur;
+  const int nb = gridDim.x, b = blockIdx.x;
+  partials += (int64_t)b * 10 * nblocks;
   for (int k = 0; k < 10; ++k) {
     double x = 0.0;
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
@@ -302,25 +341,34 @@ static __global__ void __launch_bounds__(kBlock) finalize_norms_kernel(
     if (threadIdx.x < 32) {
       x = lane < kBlock / 32 ? sh[lane] : 0.0;
       x = k < 5 ? warp_sum(x) : warp_max(x);
-      if (lane == 0 && it < hist_cap) hist[it * 10 + k] = k < 5 ? sqrt(x) : x;
+      if (lane == 0 && it < hist_cap) hist[(it * nb + b) * 10 + k] = k < 5 ? sqrt(x) : x;
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) *iter_ctr = it + 1;
 }
 
 static __global__ void reset_dtmin_kernel(unsigned long long* dtmin) {
   *dtmin = (unsigned long long)__double_as_longlong(1e300);
 }
 
-// First node of an explicit iteration: the freestream of this step, then the step counter.
-static __global__ void freestream_step_kernel(Params prm, int64_t* step, double* pinf_dev,
-                                              unsigned long long* dtmin) {
-  double p[6];
-  freestream_at(prm, *step, p);
-  for (int i = 0; i < 6; ++i) pinf_dev[i] = p[i];
-  *step += 1;
-  *dtmin = (unsigned long long)__double_as_longlong(1e300);
+// First node of an explicit iteration (one block): every condition's freestream of this step
+// and global-time-step reset, then the step counter and the history row.
+static __global__ void freestream_step_kernel(Params prm, int nb, int64_t* step, double* pinf_dev,
+                                              unsigned long long* dtmin, int64_t* iter_ctr,
+                                              int64_t* iter_cur) {
+  const int64_t st = *step;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    double p[6];
+    freestream_from(prm.pinf0_dev + 6 * b, prm.ramp_steps, prm.ramp_frac, st, p);
+    for (int i = 0; i < 6; ++i) pinf_dev[6 * b + i] = p[i];
+    dtmin[b] = (unsigned long long)__double_as_longlong(1e300);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *step = st + 1;
+    *iter_cur = *iter_ctr;
+    *iter_ctr += 1;
+  }
 }
 
 }  // namespace bes

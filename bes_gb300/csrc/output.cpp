@@ -151,7 +151,8 @@ int bes_write_host(const bes_mesh_arrays* mesh, const bes_options* opt, const do
 
 int bes_write(bes_ctx* ctx, const char* path, int32_t kind) {
   if (!ctx || !path) return BES_ERR_INVALID;
-  std::vector<double> U((size_t)ctx->soa.nc * 5);
+  // batched contexts: the first condition
+  std::vector<double> U((size_t)ctx->soa.nc * 5 * ctx->nb);
   int rc = bes_get_state(ctx, U.data());
   if (rc) return rc;
   OutMesh m{&ctx->ref, ctx->nodes.data(), (int64_t)(ctx->nodes.size() / 3), ctx->tets.data()};
@@ -163,6 +164,10 @@ int bes_write(bes_ctx* ctx, const char* path, int32_t kind) {
 
 int bes_solve(bes_ctx* ctx, const bes_output* out) {
   if (!ctx || !out) return BES_ERR_INVALID;
+  if (ctx->nb != 1) {
+    ctx->last_error = "bes_solve runs single-condition contexts (bes_sweep_run runs batches)";
+    return BES_ERR_UNSUPPORTED;
+  }
   const bes_options& o = ctx->opt;
   const int64_t nsteps = o.number_of_time_step;
   const bool implicit = o.solver_type == 1;

@@ -28,6 +28,7 @@ EXPORTED = [
     "bes_residual_norms_static", "bes_implicit_steps", "bes_implicit_assemble",
     "bes_ilu_order", "bes_counters", "bes_wall_force", "bes_profile",
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
+    "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
 ]
 
 OUTPUT_VTK, OUTPUT_CSV, OUTPUT_SLIP_WALL_CSV = 0, 1, 2
@@ -127,6 +128,12 @@ def load(path: str = LIB_PATH):
                                  ctypes.c_char_p, ctypes.c_int32, ctypes.c_char_p,
                                  ctypes.c_size_t]
     L.bes_solve.argtypes = [P, ctypes.POINTER(Output)]
+    L.bes_create_batch.argtypes = [ctypes.POINTER(MeshArrays), ctypes.POINTER(Options),
+                                   ctypes.c_int32, D, ctypes.POINTER(P)]
+    L.bes_conditions.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
+    L.bes_set_active.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
+    L.bes_sweep_run.argtypes = [P, ctypes.c_int64, ctypes.c_double, ctypes.c_int64,
+                                ctypes.POINTER(ctypes.c_int64), D]
     I64 = ctypes.POINTER(ctypes.c_int64)
     L.bes_host_geometry.argtypes = [ctypes.POINTER(MeshArrays), ctypes.c_int32, I64, I64, D, D, D,
                                     D, I64, I64, I64, I64, I64, I64, ctypes.c_char_p,
@@ -283,16 +290,27 @@ def read_gmsh(path: str):
 
 
 class Context:
-    """One mesh + options on the current CUDA device (the reference's Solver objects)."""
+    """One mesh + options on the current CUDA device (the reference's Solver objects).  With
+    `machs` ([n_cond][3]) the context holds a batch of freestream conditions
+    (bes_create_batch); state, histories and forces then carry a leading condition axis."""
 
-    def __init__(self, mesh, options: Options):
+    def __init__(self, mesh, options: Options, machs=None):
         L = load()
         self._mesh = _MeshKeep(mesh)
         self.options = options
         h = ctypes.c_void_p()
-        rc = L.bes_create(ctypes.byref(self._mesh.c), ctypes.byref(options), ctypes.byref(h))
+        if machs is None:
+            self.n_cond = 1
+            self.batched = False
+            rc = L.bes_create(ctypes.byref(self._mesh.c), ctypes.byref(options), ctypes.byref(h))
+        else:
+            m = np.ascontiguousarray(machs, dtype=np.float64).reshape(-1, 3)
+            self.n_cond = m.shape[0]
+            self.batched = True
+            rc = L.bes_create_batch(ctypes.byref(self._mesh.c), ctypes.byref(options),
+                                    self.n_cond, _d(m), ctypes.byref(h))
         if rc != BES_OK:
-            raise BesError(rc, "bes_create failed (mesh or CUDA device)")
+            raise BesError(rc, "bes_create failed (mesh, options or CUDA device)")
         self.h = h
         nc, nf = ctypes.c_int64(), ctypes.c_int64()
         L.bes_sizes(self.h, ctypes.byref(nc), ctypes.byref(nf))
@@ -316,12 +334,15 @@ class Context:
     def set_freestream_state(self):
         self._check(load().bes_set_freestream_state(self.h))
 
+    def _shape(self, *tail):
+        return ((self.n_cond,) if self.batched else ()) + tail
+
     def set_state(self, U):
-        U = np.ascontiguousarray(U, dtype=np.float64).reshape(self.n_cells, 5)
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(self.n_cond * self.n_cells, 5)
         self._check(load().bes_set_state(self.h, _d(U)))
 
     def get_state(self) -> np.ndarray:
-        U = np.zeros((self.n_cells, 5))
+        U = np.zeros(self._shape(self.n_cells, 5))
         self._check(load().bes_get_state(self.h, _d(U)))
         return U
 
@@ -336,7 +357,7 @@ class Context:
         return o
 
     def explicit_iterations(self, n: int, history: bool = True):
-        h = np.zeros((n, 10)) if history else None
+        h = np.zeros((n,) + self._shape(10)) if history else None
         self._check(load().bes_explicit_iterations(self.h, int(n), _d(h)))
         return h
 
@@ -390,8 +411,21 @@ class Context:
         """bes_solve: number_of_time_step steps with the reference's residual.csv and files."""
         self._check(load().bes_solve(self.h, ctypes.byref(output or default_output())))
 
+    def set_active(self, active):
+        a = np.ascontiguousarray(active, dtype=np.int32)
+        self._check(load().bes_set_active(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+
+    def sweep_run(self, max_iter: int, drop: float = 1e-8, check_every: int = 50):
+        """bes_sweep_run: iterate every condition to a residual drop; returns (iterations,
+        final relative residual) per condition."""
+        it = np.zeros(self.n_cond, np.int64)
+        fd = np.zeros(self.n_cond)
+        self._check(load().bes_sweep_run(self.h, int(max_iter), float(drop), int(check_every),
+                                         _i(it), _d(fd)))
+        return it, fd
+
     def wall_force(self) -> np.ndarray:
-        f = np.zeros(3)
+        f = np.zeros(self._shape(3))
         self._check(load().bes_wall_force(self.h, _d(f)))
         return f
 

@@ -107,8 +107,8 @@ int bes_sizes(const bes_ctx* ctx, int64_t* n_cells, int64_t* n_faces);
 
 /* Solver::setUniversalInitialCondition with the freestream primitives (include/Solver.hpp:71). */
 int bes_set_freestream_state(bes_ctx* ctx);
-int bes_set_state(bes_ctx* ctx, const double* U);  /* [n_cells][5] */
-int bes_get_state(bes_ctx* ctx, double* U);        /* [n_cells][5] */
+int bes_set_state(bes_ctx* ctx, const double* U);  /* [n_cond][n_cells][5] */
+int bes_get_state(bes_ctx* ctx, double* U);        /* [n_cond][n_cells][5] */
 
 /* Operators at the current state (the reference operator classes):
  *   TimeStepCalculator::computeAllTimeStep + getTimeStep (TimeStepCalculator.hpp:43-46)
@@ -121,7 +121,8 @@ int bes_compute_operators(bes_ctx* ctx, double cfl, double* dt, double* grad, do
                           double* face_UL, double* face_UR, double* face_flux, double* residual);
 
 /* n explicit multi-step iterations (SolverExplicit::timeStep_, src/SolverExplicit.cpp:259-393).
- * history (may be NULL): [n][10] = L2 and max norm per variable of the last stage's R. */
+ * history (may be NULL): [n][n_cond][10] = L2 and max norm per variable of the last stage's R
+ * (zeros for a frozen condition). */
 int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
 
 /* n implicit pseudo-time steps (SolverImplicit::timeStep_, src/SolverImplicit.cpp:293-345):
@@ -193,7 +194,32 @@ int bes_residual_norms_static(const double* residual, int64_t n_cells, double* n
 /* Integrated slip-wall pressure force F = sum over slip-wall faces of p S (owner-cell
  * pressure, dimensional face normal S, non-dimensional units), the quantity behind the
  * reference's slip-wall output (src/SolutionSnapshot.cpp:268-309).  force [3]. */
-int bes_wall_force(bes_ctx* ctx, double* force);
+int bes_wall_force(bes_ctx* ctx, double* force);  /* force [n_cond][3] */
+
+/* ---- Batched freestream sweep ----------------------------------------------------------
+ * n_cond freestream conditions on one mesh in one context (no reference counterpart: the
+ * reference runs one condition per process).  The mesh, geometry and graphs are shared; every
+ * per-condition array holds n_cond copies, every explicit kernel takes the condition from its
+ * grid's y index, and one graph launch advances all conditions by one iteration.  State
+ * arrays are [n_cond][n_cells][5], histories [n][n_cond][10], wall forces [n_cond][3].
+ * Explicit solver only (solver_type 0) for n_cond > 1; bes_compute_operators and bes_solve
+ * need n_cond = 1; bes_write writes condition 0.  mach [n_cond][3] replaces FREESTREAM_MACH. */
+int bes_create_batch(const bes_mesh_arrays* mesh, const bes_options* opt, int32_t n_cond,
+                     const double* mach, bes_ctx** out);
+int bes_conditions(const bes_ctx* ctx, int32_t* n_cond);
+
+/* Freeze (0) or run (1) each condition, active [n_cond]: a frozen condition's kernels return
+ * at once and its state is carried over unchanged. */
+int bes_set_active(bes_ctx* ctx, const int32_t* active);
+
+/* Run every condition until its residual L2 (all five variables, relative to its first
+ * iteration of this call) drops by `drop`, or max_iter iterations.  Convergence is checked
+ * every check_every iterations; converged conditions are frozen from then on.  iters [n_cond]
+ * receives the iteration at which each condition met the drop (max_iter if it did not),
+ * final_drop [n_cond] its last relative residual.  All conditions are active again on
+ * return.  Either output may be NULL. */
+int bes_sweep_run(bes_ctx* ctx, int64_t max_iter, double drop, int64_t check_every,
+                  int64_t* iters, double* final_drop);
 
 /* Counters of the context: out[0] kernels launched (graph kernel nodes counted per graph
  * launch), out[1] explicit iterations, out[2] implicit steps, out[3] linear iterations,

@@ -72,7 +72,7 @@ OUTPUT_CASES = {
                             4, "explicit"),
     "output_implicit_vtk": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
                             dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
-                                 mach=(0.84, 0, 0), smoother="ILU0", lin_tol=1e-2,
+                                 mach=(0.84, 0, 0), smoother="DAMPED_JACOBI", lin_tol=1e-2,
                                  lin_maxiter=300, out_format="VTK", out_slip="YES"),
                             4, "implicit"),
 }
