@@ -29,6 +29,9 @@ EXPORTED = [
     "bes_ilu_order", "bes_counters", "bes_wall_force", "bes_profile",
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
     "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
+    "bes_mlp_create", "bes_mlp_destroy", "bes_mlp_last_error", "bes_mlp_train", "bes_mlp_infer",
+    "bes_mlp_init_state", "bes_mlp_params", "bes_mlp_features", "bes_mlp_loss_grad",
+    "bes_mlp_apply_grad", "bes_mlp_normalisation",
 ]
 
 OUTPUT_VTK, OUTPUT_CSV, OUTPUT_SLIP_WALL_CSV = 0, 1, 2
@@ -134,6 +137,22 @@ def load(path: str = LIB_PATH):
     L.bes_set_active.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
     L.bes_sweep_run.argtypes = [P, ctypes.c_int64, ctypes.c_double, ctypes.c_int64,
                                 ctypes.POINTER(ctypes.c_int64), D]
+    F32 = ctypes.POINTER(ctypes.c_float)
+    I64p = ctypes.POINTER(ctypes.c_int64)
+    L.bes_mlp_create.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(P)]
+    L.bes_mlp_destroy.argtypes = [P]
+    L.bes_mlp_destroy.restype = None
+    L.bes_mlp_last_error.argtypes = [P]
+    L.bes_mlp_last_error.restype = ctypes.c_char_p
+    L.bes_mlp_train.argtypes = [P, ctypes.c_int32, D, D, ctypes.c_int64, ctypes.c_int32,
+                                ctypes.c_double, ctypes.c_double, ctypes.c_uint64, D]
+    L.bes_mlp_infer.argtypes = [P, ctypes.c_int32, D, D]
+    L.bes_mlp_init_state.argtypes = [P, P, ctypes.POINTER(ctypes.c_int32)]
+    L.bes_mlp_params.argtypes = [P, F32, F32, I64p]
+    L.bes_mlp_features.argtypes = [P, F32]
+    L.bes_mlp_loss_grad.argtypes = [P, ctypes.c_int32, I64p, D, D, D, F32, D]
+    L.bes_mlp_apply_grad.argtypes = [P, F32, ctypes.c_double, ctypes.c_double]
+    L.bes_mlp_normalisation.argtypes = [P, D]
     I64 = ctypes.POINTER(ctypes.c_int64)
     L.bes_host_geometry.argtypes = [ctypes.POINTER(MeshArrays), ctypes.c_int32, I64, I64, D, D, D,
                                     D, I64, I64, I64, I64, I64, I64, ctypes.c_char_p,
@@ -452,3 +471,95 @@ class Context:
         self._check(load().bes_flux_batch(self.h, int(kind), n, _d(UL), _d(UR), _d(nhat), _d(F),
                                           _d(JL), _d(JR)))
         return (F, JL, JR) if jacobians else F
+
+
+def _f(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class WarmStart:
+    """The learned warm start (bes_mlp_*) on a context's mesh."""
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        L = load()
+        h = ctypes.c_void_p()
+        rc = L.bes_mlp_create(ctx.h, int(seed), ctypes.byref(h))
+        if rc != BES_OK:
+            raise BesError(rc, "bes_mlp_create failed")
+        self.h = h
+        self.n_cells = ctx.n_cells
+        n = ctypes.c_int64()
+        L.bes_mlp_params(self.h, None, None, ctypes.byref(n))
+        self.n_params = n.value
+
+    def _check(self, rc):
+        if rc != BES_OK:
+            raise BesError(rc, load().bes_mlp_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().bes_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, np.float32)
+        self._check(load().bes_mlp_params(self.h, _f(p), None, None))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(load().bes_mlp_params(self.h, None, _f(p), None))
+
+    def features(self) -> np.ndarray:
+        x = np.zeros((self.n_cells, 3), np.float32)
+        self._check(load().bes_mlp_features(self.h, _f(x)))
+        return x
+
+    def loss_grad(self, cells, cond, targets):
+        cells = np.ascontiguousarray(cells, dtype=np.int64)
+        cond = np.ascontiguousarray(cond, dtype=np.float64)
+        targets = np.ascontiguousarray(targets, dtype=np.float64)
+        n = cells.shape[0]
+        loss = ctypes.c_double()
+        g = np.zeros(self.n_params, np.float32)
+        out = np.zeros((n, 5))
+        self._check(load().bes_mlp_loss_grad(self.h, n, _i(cells), _d(cond), _d(targets),
+                                             ctypes.byref(loss), _f(g), _d(out)))
+        return loss.value, g, out
+
+    def apply_grad(self, grad, lr: float, weight_decay: float):
+        g = np.ascontiguousarray(grad, dtype=np.float32)
+        self._check(load().bes_mlp_apply_grad(self.h, _f(g), float(lr), float(weight_decay)))
+
+    def train(self, machs, states, steps: int, batch: int = 8192, lr: float = 1e-3,
+              weight_decay: float = 1e-4, seed: int = 0):
+        machs = np.ascontiguousarray(machs, dtype=np.float64).reshape(-1, 3)
+        states = np.ascontiguousarray(states, dtype=np.float64)
+        loss = np.zeros(steps)
+        self._check(load().bes_mlp_train(self.h, machs.shape[0], _d(machs), _d(states), int(steps),
+                                         int(batch), float(lr), float(weight_decay), int(seed),
+                                         _d(loss)))
+        return loss
+
+    def infer(self, machs) -> np.ndarray:
+        machs = np.ascontiguousarray(machs, dtype=np.float64).reshape(-1, 3)
+        U = np.zeros((machs.shape[0], self.n_cells, 5))
+        self._check(load().bes_mlp_infer(self.h, machs.shape[0], _d(machs), _d(U)))
+        return U
+
+    def init_state(self, ctx: Context) -> np.ndarray:
+        used = np.zeros(ctx.n_cond, np.int32)
+        self._check(load().bes_mlp_init_state(self.h, ctx.h,
+                                              used.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+        return used
+
+    def normalisation(self) -> dict:
+        out = np.zeros(11)
+        self._check(load().bes_mlp_normalisation(self.h, _d(out)))
+        return dict(cond_mean=out[:3], cond_std=out[3:6], out_scale=out[6:])

@@ -221,6 +221,49 @@ int bes_set_active(bes_ctx* ctx, const int32_t* active);
 int bes_sweep_run(bes_ctx* ctx, int64_t max_iter, double drop, int64_t check_every,
                   int64_t* iters, double* final_drop);
 
+/* ---- Learned warm start --------------------------------------------------------------------
+ * No counterpart in the reference, which always starts from the freestream
+ * (Solver::setUniversalInitialCondition, include/Solver.hpp:71).  A coordinate MLP on the
+ * context's mesh (cell centroid -> 16 Fourier features per axis, 4 FiLM-conditioned layers of
+ * width 256 with SiLU, 5 outputs relative to the freestream) predicts the converged state for
+ * a freestream Mach vector.  It is trained on the GPU from solutions the solver produced, with
+ * BF16 tensor-core GEMMs, FP32 accumulation and AdamW on FP32 master weights; the solver then
+ * converges from the prediction (the freestream stays the fallback).  Parameters are one flat
+ * FP32 vector in the order of oracle/mlp_oracle.py layout(). */
+typedef struct bes_mlp bes_mlp;
+int bes_mlp_create(const bes_ctx* ctx, uint64_t seed, bes_mlp** out);
+void bes_mlp_destroy(bes_mlp* mlp);
+const char* bes_mlp_last_error(const bes_mlp* mlp);
+
+/* Train for `steps` AdamW steps of `batch` (cell, sample) rows drawn from n_samples solutions
+ * U [n_samples][n_cells][5] (reference numbering) at Mach vectors mach [n_samples][3].  The
+ * condition and output normalisation are taken from these samples.  loss [steps] may be NULL.
+ * batch: a multiple of 128. */
+int bes_mlp_train(bes_mlp* mlp, int32_t n_samples, const double* mach, const double* U,
+                  int64_t steps, int32_t batch, double lr, double weight_decay, uint64_t seed,
+                  double* loss);
+
+/* Predicted states U [n][n_cells][5] for Mach vectors mach [n][3]. */
+int bes_mlp_infer(bes_mlp* mlp, int32_t n, const double* mach, double* U);
+
+/* Set every condition of ctx to its predicted state; a condition whose prediction has a cell
+ * with rho <= 0 or p <= 0 gets the freestream instead.  used [n_cond] (may be NULL): 1 where
+ * the prediction was used.  Resets the context's step counters as bes_set_freestream_state. */
+int bes_mlp_init_state(bes_mlp* mlp, bes_ctx* ctx, int32_t* used);
+
+/* Checks and inspection: the flat FP32 parameters (get and/or set; n_params receives the
+ * count), the scaled centroids xn [n_cells][3], one forward + backward on given rows
+ * (cells [n_rows], normalised conditions [n_rows][3], normalised targets [n_rows][5];
+ * n_rows a multiple of 128) returning the loss, the gradient [n_params] and the outputs
+ * [n_rows][5], one AdamW step with a given gradient, and the normalisation
+ * out [11] = condition mean [3], std [3], output scale [5]. */
+int bes_mlp_params(bes_mlp* mlp, float* get, const float* set, int64_t* n_params);
+int bes_mlp_features(bes_mlp* mlp, float* xn);
+int bes_mlp_loss_grad(bes_mlp* mlp, int32_t n_rows, const int64_t* cells, const double* cond,
+                      const double* targets, double* loss, float* grad, double* outputs);
+int bes_mlp_apply_grad(bes_mlp* mlp, const float* grad, double lr, double weight_decay);
+int bes_mlp_normalisation(const bes_mlp* mlp, double* out);
+
 /* Counters of the context: out[0] kernels launched (graph kernel nodes counted per graph
  * launch), out[1] explicit iterations, out[2] implicit steps, out[3] linear iterations,
  * out[4] linear iterations whose Gram-Schmidt step needed the second pass.  out [5]. */

@@ -76,15 +76,21 @@ def test_frozen_condition_keeps_its_state():
 def test_sweep_run_stops_each_condition_at_its_drop():
     nbuild.build()
     mesh = meshgen.bump_channel(12, 4, 4, 0.08)
-    drop, max_iter = 1e-2, 300
+    max_iter = 300
+    # single runs first: a drop that every condition reaches within 200 iterations
+    singles = []
+    for mach in MACHS:
+        hs, _, _ = _single(mesh, mach, max_iter)
+        r = np.sqrt((hs[:, :5] ** 2).sum(axis=1))
+        singles.append(r)
+    drop = max(float(np.min(r[:200] / r[0])) for r in singles) * (1 + 1e-9)
     ctx = lib.Context(mesh, _opts(), machs=MACHS)
     iters, final = ctx.sweep_run(max_iter, drop=drop, check_every=1)
     U = ctx.get_state()
     for b, mach in enumerate(MACHS):
-        hs, _, _ = _single(mesh, mach, max_iter)
-        r = np.sqrt((hs[:, :5] ** 2).sum(axis=1))
+        r = singles[b]
         hit = np.nonzero(r <= drop * r[0])[0]
-        assert hit.size, "the single run should reach the drop within max_iter"
+        assert hit.size and hit[0] < 200
         assert iters[b] == hit[0] + 1
         assert final[b] == pytest.approx(r[hit[0]] / r[0], rel=1e-12)
         _, Us, _ = _single(mesh, mach, int(iters[b]))
