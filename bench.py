@@ -276,7 +276,8 @@ def implicit_leg(args, torch, ctx, steps, warmup, flush, with_e2e):
     c1 = ctx.counters()
     dev_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
     out = dict(ms=dev_ms, hist=np.array(hist), prof=prof,
-               launches=c1["launches"] - c0["launches"])
+               launches=c1["launches"] - c0["launches"], state=ctx.get_state(),
+               force=ctx.wall_force())
     if with_e2e:
         U = ctx.get_state()
         t0 = time.perf_counter()
@@ -370,10 +371,16 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
                            "ms_per_step": plain["ms"] / args.steps,
                            "linear_iterations_per_step": float(plain["hist"][:, 12].mean()),
                            "mixed_over_fp64": plain["ms"] / mixed["ms"]},
+            # the FP32-system run against the FP64-system run after the same steps
+            "error_vs_fp64": {
+                "state_rel_l2": float(np.linalg.norm(mixed["state"] - plain["state"])
+                                      / np.linalg.norm(plain["state"])),
+                "force_rel": float(np.linalg.norm(mixed["force"] - plain["force"])
+                                   / np.linalg.norm(plain["force"]))},
             "e2e": {"value": world * nc * args.steps / e2e_s, "unit": METRIC,
                     "h2d_bytes_per_step": 40 * nc, "d2h_bytes_per_step": 40 * nc},
             "gpu_launches": mixed["launches"],
-            "roofline": {"kernel": {"precond": "block-ILU(0) sweeps (ilu_lower/upper_kernel)",
+            "roofline": {"kernel": {"precond": "block-ILU(0) colour sweeps (ilu_colour_kernel)",
                                     "spmv": "spmv_kernel"}[dom],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
