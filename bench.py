@@ -76,6 +76,20 @@ WORKLOADS = {
                                             gmres_restart=30, cfl_ramp_steps=50,
                                             cfl_ramp_start=10.0, cfl_ramp_end=1000.0,
                                             precision=0)),
+    # batched sweep: 64 freestream conditions (numpy seed 0: Mach 0.3-0.85, pitch and sideslip
+    # -4..4 deg) on the 100x50x100-hex Gaussian-bump box (3.0M tets, stretching 1.05), explicit
+    # local dt at CFL 0.8, all conditions advanced by one graph launch per iteration
+    "sweep_gauss_3m_64": dict(kind="explicit", mesh=("gauss", 100, 50, 100, 1.05),
+                              conds=(0, 64),
+                              opts=dict(solver_type=0, local_time_step=1, courant_num=0.8)),
+    # learned warm start (scaled form of the survey's configuration 4): 30x15x30-hex Gaussian
+    # box (81,000 tets); training data = the batched explicit solver's states after 1500
+    # iterations for 32 conditions (seed 1); 8 held-out conditions (seed 2) run from the
+    # network's prediction and from the freestream
+    "warmstart_gauss_81k": dict(kind="warmstart", mesh=("gauss", 30, 15, 30, 1.05),
+                                train=(1, 32), test=(2, 8), data_iters=1500, eval_iters=1500,
+                                train_steps=3000, batch=8192,
+                                opts=dict(solver_type=0, local_time_step=1, courant_num=0.8)),
     # same scheme on the 200x60x30-hex channel (2.16M tets), Mach 0.84
     "explicit_bump_2m": dict(kind="explicit", mesh=("bump", 200, 60, 30, 0.08),
                              opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
@@ -176,12 +190,14 @@ def traffic_from_profiles(kernel: str, workload: str):
     return d.get(workload, {}).get(kernel)
 
 
-def cpu_baseline(wl, mesh, steps: int = 2):
-    """The CPU restatement (reference operation order, OpenMP on all host cores)."""
+def cpu_baseline(wl, mesh, steps: int = 2, mach=None):
+    """The CPU restatement (reference operation order, OpenMP on all host cores), one
+    condition."""
     from oracle import pyoracle
     o = wl["opts"]
     threads = os.cpu_count() or 1
-    O = pyoracle.Oracle(mesh, cfl=o["courant_num"], mach=o["freestream_mach"],
+    mach = o["freestream_mach"] if mach is None else tuple(mach)
+    O = pyoracle.Oracle(mesh, cfl=o["courant_num"], mach=mach,
                         local_dt=o["local_time_step"], threads=threads)
     O.explicit_run(1)  # warm-up
     t0 = time.perf_counter()
@@ -215,7 +231,12 @@ def run_reference(args, wl):
     from oracle import pyoracle
     o = wl["opts"]
     threads = os.cpu_count() or 1
-    O = pyoracle.Oracle(mesh, cfl=o["courant_num"], mach=o["freestream_mach"],
+    mach = o.get("freestream_mach")
+    if mach is None:  # a sweep: the reference runs one condition per process, time the first
+        from bes_gb300 import meshgen
+        seed, n = wl["conds"]
+        mach = meshgen.freestream_mach_vector(*meshgen.sample_conditions(n, seed)[0])
+    O = pyoracle.Oracle(mesh, cfl=o["courant_num"], mach=mach,
                         local_dt=o["local_time_step"], threads=threads)
     O.explicit_run(max(1, min(args.warmup, 2)))
     # each step: one full explicit iteration on the whole mesh; bounded to about 3 minutes
@@ -393,6 +414,76 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
     return line
 
 
+def run_warmstart(args, wl, torch, mesh, clocks):
+    """Train the warm start on the batched solver's states and compare, on held-out
+    conditions, the iterations needed to reach a residual target from the prediction and from
+    the freestream.  value: cell-updates/s of the held-out batch started from the prediction."""
+    from bes_gb300 import lib, meshgen
+
+    def machs(seed, n):
+        return np.array([meshgen.freestream_mach_vector(*c)
+                         for c in meshgen.sample_conditions(n, seed)])
+
+    opts = lib.default_options(**wl["opts"])
+    train, test = machs(*wl["train"]), machs(*wl["test"])
+    t0 = time.perf_counter()
+    data = lib.Context(mesh, opts, machs=train)
+    data.explicit_iterations(wl["data_iters"], history=False)
+    states = data.get_state()
+    data.close()
+    t_data = time.perf_counter() - t0
+    base = lib.Context(mesh, opts)
+    net = lib.WarmStart(base, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = net.train(train, states, steps=wl["train_steps"], batch=wl["batch"], lr=1e-3,
+                     weight_decay=1e-4, seed=1)
+    t_train = time.perf_counter() - t0
+    n_it = wl["eval_iters"]
+    fs = lib.Context(mesh, opts, machs=test)
+    h_fs = fs.explicit_iterations(n_it)
+    U_ref = fs.get_state()
+    fs.close()
+    warm = lib.Context(mesh, opts, machs=test)
+    used = net.init_state(warm)
+    U0 = warm.get_state()
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h_w = warm.explicit_iterations(n_it)
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    clk = clocks.stop()
+    r_fs = np.sqrt((h_fs[:, :, :5] ** 2).sum(axis=2))
+    r_w = np.sqrt((h_w[:, :, :5] ** 2).sum(axis=2))
+    target = r_fs[n_it // 2]
+    it_fs = [int(np.argmax(r_fs[:, b] <= target[b]) + 1) for b in range(len(test))]
+    it_w = [int(np.argmax(r_w[:, b] <= target[b]) + 1) if (r_w[:, b] <= target[b]).any()
+            else None for b in range(len(test))]
+    err_pred = np.linalg.norm((U0 - U_ref).reshape(len(test), -1), axis=1) / \
+        np.linalg.norm(U_ref.reshape(len(test), -1), axis=1)
+    nc = warm.n_cells
+    warm.close()
+    net.close()
+    base.close()
+    value = len(test) * nc * n_it / t_warm
+    return {"metric": METRIC, "metric_full": METRIC_FULL, "value": value, "unit": METRIC,
+            "n_gpus": 1, "steps": n_it, "warmup": 0, "ms_per_step": t_warm / n_it * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "cells": nc, "train_conditions": len(train),
+                       "test_conditions": len(test), "parallelism": "replicas1",
+                       "l2": "not flushed (wall clock of a whole batched run)"},
+            "warm_start": {
+                "iterations_to_target_freestream": it_fs, "iterations_to_target_warm": it_w,
+                "target": "the freestream run's residual L2 at iteration %d" % (n_it // 2),
+                "prediction_rel_error_vs_state_at_%d" % n_it: [float(x) for x in err_pred],
+                "prediction_used": [int(x) for x in used],
+                "train_seconds": t_train, "data_seconds": t_data,
+                "final_loss": float(loss[-100:].mean()), "first_loss": float(loss[:10].mean())},
+            "clocks": clk}
+
+
 def run_converge(args, wl, ctx, max_steps: int, drop: float = 1e-8):
     """Implicit steps until the L2 of the unscaled residual (all variables) falls by `drop`
     relative to the first step; returns steps, device-synchronous wall time and the history."""
@@ -450,8 +541,20 @@ def main():
     from bes_gb300 import lib
     nbuild.build()
     mesh = make_mesh(wl["mesh"])
-    ctx = lib.Context(mesh, lib.default_options(**wl["opts"]))
+    if wl["kind"] == "warmstart":
+        line = run_warmstart(args, wl, torch, mesh, ClockSampler(local_rank))
+        if rank == 0:
+            print(json.dumps(line))
+        return 0
+    machs = None
+    if "conds" in wl:
+        from bes_gb300 import meshgen
+        seed, n = wl["conds"]
+        machs = np.array([meshgen.freestream_mach_vector(*c)
+                          for c in meshgen.sample_conditions(n, seed)])
+    ctx = lib.Context(mesh, lib.default_options(**wl["opts"]), machs=machs)
     nc, nf = ctx.n_cells, ctx.n_faces
+    ncond = ctx.n_cond
     if wl["kind"] == "implicit":
         line = run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist)
         if args.converge:
@@ -498,7 +601,7 @@ def main():
         tt = torch.tensor([dev_ms], dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max = float(tt.item())
-    value = world * nc * args.steps / (t_max / 1e3)
+    value = world * ncond * nc * args.steps / (t_max / 1e3)
 
     # end to end through the C ABI with host buffers
     U = ctx.get_state()
@@ -513,15 +616,15 @@ def main():
         tt = torch.tensor([e2e_s], dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e2e_max = float(tt.item())
-    e2e = world * nc * args.steps / e2e_max
+    e2e = world * ncond * nc * args.steps / e2e_max
 
     n_stage = 4
     per_launch = {"cell_recon_kernel": kms[0] / (args.steps * n_stage),
                   "face_flux_kernel": kms[1] / (args.steps * n_stage),
                   "update_kernel": kms[2] / (args.steps * n_stage)}
-    bytes_per_launch = {"cell_recon_kernel": BYTES_PER_CELL_SWEEP * nc,
-                        "face_flux_kernel": BYTES_PER_FACE * nf,
-                        "update_kernel": BYTES_PER_UPDATE * nc}
+    bytes_per_launch = {"cell_recon_kernel": BYTES_PER_CELL_SWEEP * nc * ncond,
+                        "face_flux_kernel": BYTES_PER_FACE * nf * ncond,
+                        "update_kernel": BYTES_PER_UPDATE * nc * ncond}
     dom = max(per_launch, key=lambda k: per_launch[k])
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_launch[dom] / (per_launch[dom] / 1e3) / 1e9
@@ -537,13 +640,13 @@ def main():
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "cells": nc, "faces": nf,
-                       "parallelism": f"replicas{world}",
+                       "conditions": ncond, "parallelism": f"replicas{world}",
                        "l2": "flushed before every timed step (256 MB write)"},
-            "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": 40 * nc,
-                    "d2h_bytes_per_step": 40 * nc + 80 + 4},
+            "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": 40 * nc * ncond,
+                    "d2h_bytes_per_step": (40 * nc + 80) * ncond + 4},
             "gpu_launches": 14 * args.steps, "roofline": roof, "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(wl, mesh)
+        line["cpu_baseline"] = cpu_baseline(wl, mesh, mach=None if machs is None else machs[0])
     ctx.close()
     if rank == 0:
         print(json.dumps(line))
