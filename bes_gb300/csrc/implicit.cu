@@ -117,7 +117,7 @@ void enqueue_ilu_factor(const Sys<T>& S) {
   }
 }
 
-// Colour-range sweeps (ilu_colour5_kernel) from `in` into S.Z: colours 1..C-2 forward, the last
+// Colour-range sweeps (ilu_colour_kernel) from `in` into S.Z: colours 1..C-2 forward, the last
 // colour's two solves fused, colours C-2..0 backward.
 template <class T>
 void enqueue_ilu_colour_sweeps(const Sys<T>& S, const T* in) {
@@ -125,20 +125,19 @@ void enqueue_ilu_colour_sweeps(const Sys<T>& S, const T* in) {
   const SoaMesh& M = c->soa;
   const int C = M.n_stages;
   const int s1 = M.stage_off[1];
-  const dim3 blk(32, 5);
   auto range = [&](int k, int& r0, int& r1) { r0 = M.stage_off[k]; r1 = M.stage_off[k + 1]; };
   int r0, r1;
   for (int k = 1; k < C - 1; ++k) {
     range(k, r0, r1);
-    ilu_colour5_kernel<T, true, false><<<nblk(r1 - r0, 32), blk, 0, S.s>>>(
+    ilu_colour_kernel<T, true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
         c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
   }
   range(C - 1, r0, r1);
-  ilu_colour5_kernel<T, true, true><<<nblk(r1 - r0, 32), blk, 0, S.s>>>(c->dm, r0, r1, s1, S.LU,
+  ilu_colour_kernel<T, true, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(c->dm, r0, r1, s1, S.LU,
                                                                        S.Dinv, in, S.Z);
   for (int k = C - 2; k >= 0; --k) {
     range(k, r0, r1);
-    ilu_colour5_kernel<T, false, true><<<nblk(r1 - r0, 32), blk, 0, S.s>>>(
+    ilu_colour_kernel<T, false, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
         c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
   }
 }

@@ -438,50 +438,6 @@ __global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int 
   }
 }
 
-// The same colour-range sweep with five threads per row: block (32, 5), warp r computes
-// component r of 32 consecutive rows (the per-component operation order of
-// ilu_colour_kernel), so a colour of ~1/5 of the cells keeps five times as many loads in
-// flight; the inverse-diagonal product exchanges the five components through shared memory.
-template <class T, bool LOWER, bool UPPER>
-__global__ void __launch_bounds__(160) ilu_colour5_kernel(DevMesh m, int r0, int r1, int s1,
-                                                          const T* __restrict__ A,
-                                                          const T* __restrict__ Dinv,
-                                                          const T* __restrict__ in,
-                                                          T* __restrict__ out) {
-  __shared__ T sh[5][32];
-  const int i = r0 + blockIdx.x * 32 + threadIdx.x;
-  const int r = threadIdx.y;
-  const bool valid = i < r1;
-  const int nc = m.nc;
-  T acc = T(0);
-  if (valid) {
-    const T* own = (LOWER || r0 == 0) ? in : out;
-    acc = own[(int64_t)r * nc + i];
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      const int j = m.adj[s * nc + i];
-      const bool lower = LOWER && j >= 0 && j < r0;
-      const bool upper = UPPER && j >= r1;
-      if (!lower && !upper) continue;
-      const T* src = (lower && j < s1) ? in : out;
-#pragma unroll
-      for (int c = 0; c < 5; ++c) acc -= ellc(A, 1 + s, r * 5 + c, nc, i) * src[(int64_t)c * nc + j];
-    }
-  }
-  if (UPPER) {
-    sh[r][threadIdx.x] = acc;
-    __syncthreads();
-    if (valid) {
-      T x = T(0);
-#pragma unroll
-      for (int c = 0; c < 5; ++c) x += Dinv[(int64_t)(r * 5 + c) * nc + i] * sh[c][threadIdx.x];
-      out[(int64_t)r * nc + i] = x;
-    }
-  } else if (valid) {
-    out[(int64_t)r * nc + i] = acc;
-  }
-}
-
 // block-Jacobi application: out_i = Dinv_i in_i
 template <class T>
 __global__ void __launch_bounds__(256) jacobi_apply_kernel(int nc, const T* __restrict__ Dinv,
