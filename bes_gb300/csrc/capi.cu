@@ -187,7 +187,6 @@ int bes_create(const bes_mesh_arrays* mesh, const bes_options* opt, bes_ctx** ou
 int bes_create_batch(const bes_mesh_arrays* mesh, const bes_options* opt, int32_t n_cond,
                      const double* mach, bes_ctx** out) {
   if (!opt || !mach || n_cond < 1) return BES_ERR_INVALID;
-  if (opt->solver_type != 0 && n_cond > 1) return BES_ERR_UNSUPPORTED;
   return create_context(mesh, opt, n_cond, mach, out);
 }
 
@@ -285,6 +284,7 @@ int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_co
   BES_CUDA_TRY(c, cudaMemcpy(c->pinf0_dev, c->pinf0_host.data(), 6 * nb * sizeof(double),
                              cudaMemcpyHostToDevice));
   c->active_host.assign(nb, 1);
+  if (nb > 1) c->cond_imp.assign(nb, bes_ctx::CondImplicit());
   BES_CUDA_TRY(c, cudaMemcpy(c->active_dev, c->active_host.data(), nb * sizeof(int32_t),
                              cudaMemcpyHostToDevice));
   c->prm.pinf_dev = c->pinf_dev;
@@ -341,6 +341,10 @@ int bes_set_freestream_state(bes_ctx* ctx) {
   ctx->imp.step_count = 0;
   ctx->imp.cfl_actual = ctx->opt.courant_num;
   for (int v = 0; v < 5; ++v) ctx->imp.maxres[v] = ctx->imp.maxres_old[v] = 0.0;
+  for (auto& ci : ctx->cond_imp) {
+    ci = bes_ctx::CondImplicit();
+    ci.cfl_actual = ctx->opt.courant_num;
+  }
   const int64_t zero = 0;
   BES_CUDA_TRY(ctx, cudaMemcpy(ctx->step_dev, &zero, sizeof(zero), cudaMemcpyHostToDevice));
   // GasPerfect_::computeAllConservedVariable of the step-0 freestream primitives

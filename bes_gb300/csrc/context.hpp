@@ -153,6 +153,16 @@ struct bes_ctx {
   int32_t* active_dev = nullptr;     // [nb]
   std::vector<double> pinf0_host;    // [nb][6]
   std::vector<int32_t> active_host;  // [nb]
+  // implicit batches step the conditions one after another through one set of implicit
+  // buffers; each condition keeps its own CFL controller and step counters
+  struct CondImplicit {
+    double cfl_actual = 0;
+    double maxres[5] = {0, 0, 0, 0, 0};
+    double maxres_old[5] = {0, 0, 0, 0, 0};
+    int64_t step_count = 0;
+    int64_t host_step = 0;
+  };
+  std::vector<CondImplicit> cond_imp;  // [nb] when nb > 1
   int* nan_flag = nullptr;  // face index + 1 of a NaN flux (0 none)
   double* pinf_dev = nullptr;     // [6] freestream primitives of the current step
   int64_t* step_dev = nullptr;    // solver step counter read by the explicit graphs

@@ -437,6 +437,74 @@ int implicit_step(bes_ctx* c, double* hist) {
   return BES_OK;
 }
 
+// A batched context's condition b seen as a single-condition context: its state, face
+// states, fluxes, time steps and freestream, and its CFL controller, swapped in for the
+// duration of one implicit step (the implicit buffers are shared by all conditions).
+struct ConditionView {
+  bes_ctx* c;
+  double* U[2];
+  double *RS, *FA, *dt, *pinf;
+  unsigned long long* dtmin;
+  Params prm;
+  bes_ctx::CondImplicit saved;
+  int nb;
+  ConditionView(bes_ctx* ctx, int b) : c(ctx) {
+    const int64_t nc = c->soa.nc, nf = c->soa.nf;
+    for (int k = 0; k < 2; ++k) U[k] = c->U[k];
+    RS = c->RS; FA = c->FA; dt = c->dt; pinf = c->pinf_dev; dtmin = c->dtmin;
+    prm = c->prm;
+    nb = c->nb;
+    for (int k = 0; k < 2; ++k) c->U[k] += (int64_t)b * 5 * nc;
+    c->RS += (int64_t)b * 5 * c->rs_ld;
+    c->FA += (int64_t)b * 5 * nf;
+    c->dt += (int64_t)b * nc;
+    c->dtmin += b;
+    c->pinf_dev += 6 * b;
+    c->prm.pinf_dev = c->pinf_dev;
+    c->prm.active = nullptr;
+    for (int i = 0; i < 6; ++i) c->prm.pinf[i] = c->pinf0_host[6 * b + i];
+    c->nb = 1;
+    swap_scalars(c->cond_imp[b]);
+  }
+  void swap_scalars(bes_ctx::CondImplicit& s) {
+    ImplicitBuffers& I = c->imp;
+    std::swap(s.cfl_actual, I.cfl_actual);
+    for (int v = 0; v < 5; ++v) {
+      std::swap(s.maxres[v], I.maxres[v]);
+      std::swap(s.maxres_old[v], I.maxres_old[v]);
+    }
+    std::swap(s.step_count, I.step_count);
+    std::swap(s.host_step, c->host_step);
+  }
+  void release(int b) {
+    swap_scalars(c->cond_imp[b]);
+    for (int k = 0; k < 2; ++k) c->U[k] = U[k];
+    c->RS = RS; c->FA = FA; c->dt = dt; c->pinf_dev = pinf; c->dtmin = dtmin;
+    c->prm = prm;
+    c->nb = nb;
+  }
+};
+
+// n implicit steps of every condition of a batch, condition after condition within a step;
+// history [n][nb][19]
+int implicit_steps_batch(bes_ctx* ctx, int64_t n, double* history) {
+  const int nb = ctx->nb;
+  for (int64_t i = 0; i < n; ++i) {
+    for (int b = 0; b < nb; ++b) {
+      ConditionView view(ctx, b);
+      double* h = history ? history + (i * nb + b) * 19 : nullptr;
+      const int rc = ctx->imp.prec ? implicit_step<float>(ctx, h) : implicit_step<double>(ctx, h);
+      view.release(b);
+      if (rc) return rc;
+    }
+    ++ctx->imp.step_count;
+    ++ctx->host_step;
+  }
+  IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  prof_collect(ctx);
+  return BES_OK;
+}
+
 }  // namespace
 
 namespace bes {
@@ -536,6 +604,7 @@ int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history) {
     ctx->last_error = "context was not created for the implicit solver";
     return BES_ERR_INVALID;
   }
+  if (ctx->nb > 1) return implicit_steps_batch(ctx, n, history);
   for (int64_t i = 0; i < n; ++i) {
     int rc = ctx->imp.prec ? implicit_step<float>(ctx, history ? history + i * 19 : nullptr)
                            : implicit_step<double>(ctx, history ? history + i * 19 : nullptr);
@@ -565,6 +634,10 @@ int bes_profile(bes_ctx* ctx, int32_t enable, double* ms_out, int64_t* counts_ou
 int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks, int64_t* n_blocks) {
   if (!ctx) return BES_ERR_INVALID;
   if (ctx->opt.solver_type != 1 || !ctx->imp.A) return BES_ERR_INVALID;
+  if (ctx->nb != 1) {
+    ctx->last_error = "the system is assembled on single-condition contexts";
+    return BES_ERR_UNSUPPORTED;
+  }
   const SoaMesh& M = ctx->soa;
   const RefMesh& R = ctx->ref;
   const int64_t nc = M.nc;

@@ -397,8 +397,8 @@ class Context:
         return dict(cell_ms=ms[0], face_ms=ms[1], update_ms=ms[2], total_ms=ms[3])
 
     def implicit_steps(self, n: int):
-        """n implicit steps; history [n, 19] (see bes_implicit_steps)."""
-        h = np.zeros((n, 19))
+        """n implicit steps; history [n, 19], batched [n, n_cond, 19] (see bes_implicit_steps)."""
+        h = np.zeros((n,) + self._shape(19))
         self._check(load().bes_implicit_steps(self.h, int(n), _d(h)))
         return h
 

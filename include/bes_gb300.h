@@ -125,7 +125,8 @@ int bes_compute_operators(bes_ctx* ctx, double cfl, double* dt, double* grad, do
  * (zeros for a frozen condition). */
 int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
 
-/* n implicit pseudo-time steps (SolverImplicit::timeStep_, src/SolverImplicit.cpp:293-345):
+/* (batched contexts: history [n][n_cond][19], see bes_create_batch)
+ * n implicit pseudo-time steps (SolverImplicit::timeStep_, src/SolverImplicit.cpp:293-345):
  * local/global dt at the step's CFL, second-order residual, first-order Jacobians assembled
  * into the 5x5-block system (each block added jacobian_repeat times, Q9), right-preconditioned
  * GMRES(gmres_restart) to linear_solver_tol relative with a block-Jacobi (linear_solver 0),
@@ -201,9 +202,13 @@ int bes_wall_force(bes_ctx* ctx, double* force);  /* force [n_cond][3] */
  * reference runs one condition per process).  The mesh, geometry and graphs are shared; every
  * per-condition array holds n_cond copies, every explicit kernel takes the condition from its
  * grid's y index, and one graph launch advances all conditions by one iteration.  State
- * arrays are [n_cond][n_cells][5], histories [n][n_cond][10], wall forces [n_cond][3].
- * Explicit solver only (solver_type 0) for n_cond > 1; bes_compute_operators and bes_solve
- * need n_cond = 1; bes_write writes condition 0.  mach [n_cond][3] replaces FREESTREAM_MACH. */
+ * arrays are [n_cond][n_cells][5], histories [n][n_cond][10] (explicit) or [n][n_cond][19]
+ * (implicit), wall forces [n_cond][3].  The implicit solver steps the conditions one after
+ * another through one set of implicit buffers (each condition keeps its own state, CFL
+ * controller and freestream), so a batch needs the implicit memory of one condition only.
+ * bes_compute_operators, bes_implicit_assemble and bes_solve need n_cond = 1; bes_write
+ * writes condition 0; bes_sweep_run drives the explicit solver.  mach [n_cond][3] replaces
+ * FREESTREAM_MACH. */
 int bes_create_batch(const bes_mesh_arrays* mesh, const bes_options* opt, int32_t n_cond,
                      const double* mach, bes_ctx** out);
 int bes_conditions(const bes_ctx* ctx, int32_t* n_cond);

@@ -98,11 +98,37 @@ def test_sweep_run_stops_each_condition_at_its_drop():
     ctx.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_implicit_batch_matches_single_condition_runs(precision):
+    """Implicit batches step the conditions one after another through shared implicit
+    buffers; every condition, with its own adaptive CFL, matches its own context."""
+    nbuild.build()
+    mesh = meshgen.bump_channel(12, 4, 4, 0.08)
+    kw = dict(solver_type=1, courant_num=10.0, adaptive_courant_num_max=500.0,
+              linear_solver=1, linear_solver_tol=1e-2, linear_solver_max_iter=200,
+              precision=precision)
+    ctx = lib.Context(mesh, _opts(**kw), machs=MACHS)
+    h = ctx.implicit_steps(6)
+    U = ctx.get_state()
+    assert h.shape == (6, 3, 19)
+    for b, mach in enumerate(MACHS):
+        single = lib.Context(mesh, _opts(freestream_mach=mach, **kw))
+        hs = single.implicit_steps(6)
+        assert np.array_equal(h[:, b], hs)
+        assert np.array_equal(U[b], single.get_state())
+        single.close()
+    ctx.close()
+
+
 def test_batch_rejects_what_it_does_not_run():
     nbuild.build()
     mesh = meshgen.bump_channel(6, 2, 2, 0.08)
+    imp = lib.Context(mesh, _opts(solver_type=1, linear_solver=1), machs=MACHS)
     with pytest.raises(lib.BesError, match="BES_ERR_UNSUPPORTED"):
-        lib.Context(mesh, _opts(solver_type=1), machs=MACHS)
+        imp.implicit_assemble(10.0)
+    with pytest.raises(lib.BesError, match="BES_ERR_UNSUPPORTED"):
+        imp.sweep_run(10)
+    imp.close()
     ctx = lib.Context(mesh, _opts(), machs=MACHS[:2])
     with pytest.raises(lib.BesError, match="BES_ERR_UNSUPPORTED"):
         ctx.operators(0.8)
