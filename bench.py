@@ -53,7 +53,7 @@ WORKLOADS = {
     # first-order Roe Jacobian in 5x5 blocks, block-ILU(0) GMRES(30) to 1e-2 relative, CFL
     # ramped 10 -> 1000 over 50 steps; FP32 Jacobian/preconditioner/Krylov with FP64 residual
     # and update (defect correction), or everything FP64
-    "implicit_bump_2m": dict(kind="implicit", mesh=("bump", 200, 60, 30, 0.08),
+    "implicit_bump_2m": dict(kind="implicit", mesh=("bump", 200, 60, 30, 0.08), converge=300,
                                    opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
                                              freestream_mach=(0.84, 0.0, 0.0), linear_solver=1,
                                              linear_solver_tol=1e-2, linear_solver_max_iter=300,
@@ -519,8 +519,10 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="implicit_bump_2m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--converge", type=int, default=0,
-                    help="implicit workloads: also solve to a 1e-8 residual drop (max steps)")
+    ap.add_argument("--converge", type=int, default=-1,
+                    help="implicit workloads: also solve to a 1e-8 residual drop from the "
+                         "freestream with the FP32 and the FP64 system (max steps; default: "
+                         "300 for implicit_bump_2m, 0 = off)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -557,12 +559,34 @@ def main():
     ncond = ctx.n_cond
     if wl["kind"] == "implicit":
         line = run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist)
-        if args.converge:
-            ctx.set_freestream_state()
-            ctx2 = lib.Context(mesh, lib.default_options(**wl["opts"]))
-            line["converged_solve"] = run_converge(args, wl, ctx2, args.converge)
-            ctx2.close()
-        ctx.close()
+        n_conv = args.converge if args.converge >= 0 else wl.get("converge", 0)
+        if n_conv > 0:
+            ctx.close()
+            # converged solves/hour to a 1e-8 drop: the FP32-system defect correction against
+            # the plain FP64 system, each from the freestream, and their answers compared
+            runs = {}
+            for name, prec in (("mixed", 1), ("fp64", 0)):
+                o = dict(wl["opts"])
+                o["precision"] = prec
+                c2 = lib.Context(mesh, lib.default_options(**o))
+                runs[name] = run_converge(args, wl, c2, n_conv)
+                runs[name]["state"] = c2.get_state()
+                c2.close()
+            U32, U64 = runs["mixed"].pop("state"), runs["fp64"].pop("state")
+            F32 = np.array(runs["mixed"]["wall_force"])
+            F64 = np.array(runs["fp64"]["wall_force"])
+            line["converged_solve"] = {
+                "mixed": runs["mixed"], "fp64": runs["fp64"],
+                "solves_per_hour_ratio": (runs["mixed"]["solves_per_hour"]
+                                          / runs["fp64"]["solves_per_hour"]
+                                          if runs["fp64"]["solves_per_hour"] else None),
+                "state_rel_l2_vs_fp64": float(np.linalg.norm(U32 - U64) / np.linalg.norm(U64)),
+                "force_abs_diff_vs_fp64": float(np.abs(F32 - F64).max()),
+                "force_coefficient_abs_diff_vs_fp64": float(
+                    np.abs(F32 - F64).max() / (0.5 * np.sum(np.square(wl["opts"]["freestream_mach"]))))}
+            ctx = None
+        if ctx is not None:
+            ctx.close()
         if rank == 0:
             print(json.dumps(line))
         if dist:

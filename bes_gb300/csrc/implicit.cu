@@ -409,7 +409,7 @@ int implicit_step(bes_ctx* c, double* hist) {
   rc = gmres<T>(c, iters, rel);
   if (rc) return rc;
   prof_begin(c, PROF_OTHER);
-  state_update_kernel<T><<<kRedBlocks, 256, 0, c->stream>>>(c->U[c->cur], S.X, S.N);
+  state_update_kernel<T><<<kRedBlocks, 256, 0, c->stream>>>(c->U[c->cur], S.X, (int64_t)S.nc);
   prof_end(c, PROF_OTHER);
   ++c->launches;
   IMP_TRY(c, cudaGetLastError());

@@ -6,7 +6,10 @@
 //
 // ELL layout: value q (= row*5 + col) of slot s of cell i is A[(s*25 + q)*nc + i]; slot 0 is
 // the diagonal block, slot 1+m the block coupling to the neighbour across local face m.
-// Vectors are SoA: component v of cell i is x[v*nc + i].
+// The Krylov-side vectors (right-hand side b, iterates, basis, preconditioner output) are
+// cell-major: component v of cell i is x[i*5 + v], so a neighbour's five values are one
+// 20-byte gather (SoA would touch five 32-byte sectors) while streams stay coalesced; the
+// FP64 state and residual keep the solver's [5][nc] layout.
 #pragma once
 #include "explicit_kernels.cuh"
 
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(128) cell_assemble_kernel(
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       rhs[(int64_t)v * nc + i] = b[v];
-      rhs_t[(int64_t)v * nc + i] = (T)b[v];
+      rhs_t[(int64_t)i * 5 + v] = (T)b[v];
     }
   }
   __shared__ double sh[15][4];
@@ -335,21 +338,21 @@ __global__ void __launch_bounds__(128) ilu_lower_kernel(DevMesh m, const int32_t
   const int pi = pos[i];
   T acc[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = in[(int64_t)v * nc + i];
+  for (int v = 0; v < 5; ++v) acc[v] = in[(int64_t)i * 5 + v];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const int j = m.adj[s * nc + i];
     if (j < 0 || pos[j] >= pi) continue;
     T y[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) y[v] = out[(int64_t)v * nc + j];
+    for (int v = 0; v < 5; ++v) y[v] = out[(int64_t)j * 5 + v];
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
       for (int c = 0; c < 5; ++c) acc[r] -= ellc(A, 1 + s, r * 5 + c, nc, i) * y[c];
   }
 #pragma unroll
-  for (int v = 0; v < 5; ++v) out[(int64_t)v * nc + i] = acc[v];
+  for (int v = 0; v < 5; ++v) out[(int64_t)i * 5 + v] = acc[v];
 }
 
 // backward solve of one colour, in place: z_i = inv(U_ii) (y_i - sum_{upper k} U_ik z_k)
@@ -365,14 +368,14 @@ __global__ void __launch_bounds__(128) ilu_upper_kernel(DevMesh m, const int32_t
   const int pi = pos[i];
   T acc[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = z[(int64_t)v * nc + i];
+  for (int v = 0; v < 5; ++v) acc[v] = z[(int64_t)i * 5 + v];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const int k = m.adj[s * nc + i];
     if (k < 0 || pos[k] <= pi) continue;
     T y[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) y[v] = z[(int64_t)v * nc + k];
+    for (int v = 0; v < 5; ++v) y[v] = z[(int64_t)k * 5 + v];
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -383,7 +386,7 @@ __global__ void __launch_bounds__(128) ilu_upper_kernel(DevMesh m, const int32_t
     T x = T(0);
 #pragma unroll
     for (int c = 0; c < 5; ++c) x += Dinv[(int64_t)(r * 5 + c) * nc + i] * acc[c];
-    z[(int64_t)r * nc + i] = x;
+    z[(int64_t)i * 5 + r] = x;
   }
 }
 
@@ -408,7 +411,7 @@ __global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int 
   const T* own = (LOWER || r0 == 0) ? in : out;
   T acc[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)v * nc + i];
+  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const int j = m.adj[s * nc + i];
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int 
     const T* src = (lower && j < s1) ? in : out;
     T y[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) y[v] = src[(int64_t)v * nc + j];
+    for (int v = 0; v < 5; ++v) y[v] = src[(int64_t)j * 5 + v];
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -430,11 +433,11 @@ __global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int 
       T x = T(0);
 #pragma unroll
       for (int c = 0; c < 5; ++c) x += Dinv[(int64_t)(r * 5 + c) * nc + i] * acc[c];
-      out[(int64_t)r * nc + i] = x;
+      out[(int64_t)i * 5 + r] = x;
     }
   } else {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) out[(int64_t)v * nc + i] = acc[v];
+    for (int v = 0; v < 5; ++v) out[(int64_t)i * 5 + v] = acc[v];
   }
 }
 
@@ -447,13 +450,13 @@ __global__ void __launch_bounds__(256) jacobi_apply_kernel(int nc, const T* __re
   if (i >= nc) return;
   T x[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) x[v] = in[(int64_t)v * nc + i];
+  for (int v = 0; v < 5; ++v) x[v] = in[(int64_t)i * 5 + v];
 #pragma unroll
   for (int r = 0; r < 5; ++r) {
     T acc = T(0);
 #pragma unroll
     for (int c = 0; c < 5; ++c) acc += Dinv[(int64_t)(r * 5 + c) * nc + i] * x[c];
-    out[(int64_t)r * nc + i] = acc;
+    out[(int64_t)i * 5 + r] = acc;
   }
 }
 
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restric
   if (i >= nc) return;
   T acc[5], xi[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)v * nc + i];
+  for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)i * 5 + v];
 #pragma unroll
   for (int r = 0; r < 5; ++r) {
     T s = T(0);
@@ -480,7 +483,7 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restric
     const int j = m.adj[q * nc + i];
     if (j < 0) continue;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)v * nc + j];
+    for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)j * 5 + v];
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -488,7 +491,7 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restric
   }
 #pragma unroll
   for (int r = 0; r < 5; ++r)
-    y[(int64_t)r * nc + i] = b ? b[(int64_t)r * nc + i] - acc[r] : acc[r];
+    y[(int64_t)i * 5 + r] = b ? b[(int64_t)i * 5 + r] - acc[r] : acc[r];
 }
 
 // Per-thread accumulation type of the vector kernels: the FP32 system accumulates each
@@ -803,10 +806,13 @@ __global__ void __launch_bounds__(256) norm2_kernel(const T* __restrict__ x, int
 // state update W += dW (SolverImplicit::updateSolution_, src/SolverImplicit.cpp:509-528)
 template <class T>
 __global__ void __launch_bounds__(256) state_update_kernel(double* __restrict__ U,
-                                                           const T* __restrict__ dW, int64_t N) {
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
-       idx += (int64_t)gridDim.x * blockDim.x)
-    U[idx] += (double)dW[idx];
+                                                           const T* __restrict__ dW, int64_t nc) {
+  // U is [5][nc] (the solver's layout), dW cell-major [nc][5] (the Krylov layout)
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < 5 * nc;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = idx / nc, i = idx - v * nc;
+    U[idx] += (double)dW[i * 5 + v];
+  }
 }
 
 template <class T>
