@@ -365,8 +365,12 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max = float(tt.item())
     value = world * nc * args.steps / (t_max / 1e3)
-    # e2e through the C ABI with host buffers (state up, one step, state down)
+    # e2e through the C ABI with host buffers (state up, one step, state down), on the same
+    # steps: the solve restarts from the freestream and replays the warm-up untimed
+    ctx.set_freestream_state()
+    ctx.implicit_steps(args.warmup)
     U = ctx.get_state()
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.set_state(U)
@@ -557,10 +561,14 @@ def run_production(args, wl, torch, mesh, clocks):
         F64 = c64.wall_force()
         U64 = c64.get_state()
         c64.close()
-        # from a predicted field the CFL ramp starts at 100 (10 steps to 1000)
+        # production settings: from a predicted field the CFL ramp starts at 100 (10 steps to
+        # 1000), and the linear solves stop at 1e-1 (the outer rate is set by the first-order
+        # Jacobian, so 1e-2 oversolves: on the 2.16M-cell channel 1e-1 converges to the same
+        # answer in 15.5 s instead of 22.4 s)
         c32 = lib.Context(mesh, lib.default_options(**dict(o32, freestream_mach=tuple(mach),
                                                            cfl_ramp_start=100.0,
-                                                           cfl_ramp_steps=10)))
+                                                           cfl_ramp_steps=10,
+                                                           linear_solver_tol=0.1)))
         used = int(net.init_state(c32)[0])
         s32, t32, _, r32, _ = _solve_to(c32, target, wl["max_steps"])
         F32 = c32.wall_force()

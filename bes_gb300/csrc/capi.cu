@@ -127,17 +127,6 @@ int build_graphs(bes_ctx* ctx) {
   return BES_OK;
 }
 
-// [nb][nc][5] in reference numbering -> [nb][5][nc] in the device numbering
-void fill_state_aos_to_soa(const bes_ctx* ctx, const double* U, std::vector<double>& soa) {
-  const int64_t nc = ctx->soa.nc;
-  soa.resize(5 * nc * ctx->nb);
-  for (int64_t b = 0; b < ctx->nb; ++b)
-    for (int64_t i = 0; i < nc; ++i) {
-      const int64_t c = ctx->soa.cell_new2ref[i];
-      for (int v = 0; v < 5; ++v) soa[(b * 5 + v) * nc + i] = U[(b * nc + c) * 5 + v];
-    }
-}
-
 int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_cond,
                    const double* mach, bes_ctx** out);
 
@@ -267,7 +256,15 @@ int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_co
   rc |= dev_alloc(c, &c->pinf0_dev, 6 * nb);
   rc |= dev_alloc(c, &c->active_dev, nb);
   rc |= dev_alloc(c, &c->step_dev, 1);
+  rc |= dev_alloc(c, &c->stage, 5 * nc * nb);
+  rc |= dev_alloc(c, &c->new2ref_dev, nc);
   if (rc) return BES_ERR_CUDA;
+  {
+    std::vector<int32_t> n2r(nc);
+    for (int64_t i = 0; i < nc; ++i) n2r[i] = (int32_t)S.cell_new2ref[i];
+    BES_CUDA_TRY(c, cudaMemcpy(c->new2ref_dev, n2r.data(), nc * sizeof(int32_t),
+                               cudaMemcpyHostToDevice));
+  }
   BES_CUDA_TRY(c, cudaMemset(c->iter_ctr, 0, sizeof(int64_t)));
   BES_CUDA_TRY(c, cudaMemset(c->nan_flag, 0, sizeof(int)));
   // gas and freestream (Config::initializePostMesh, src/Config.cpp:480-488), per condition
@@ -376,24 +373,27 @@ int bes_set_freestream_state(bes_ctx* ctx) {
 
 int bes_set_state(bes_ctx* ctx, const double* U) {
   if (!ctx || !U) return BES_ERR_INVALID;
-  std::vector<double> soa;
-  fill_state_aos_to_soa(ctx, U, soa);
-  BES_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->U[ctx->cur], soa.data(), soa.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  const int64_t nc = ctx->soa.nc, nb = ctx->nb;
+  BES_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->stage, U, (size_t)nb * nc * 5 * sizeof(double),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+  state_from_stage_kernel<<<1024, 256, 0, ctx->stream>>>((int)nc, (int)nb, ctx->new2ref_dev,
+                                                         ctx->stage, ctx->U[ctx->cur]);
+  ++ctx->launches;
   BES_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  BES_CUDA_TRY(ctx, cudaGetLastError());
   return BES_OK;
 }
 
 int bes_get_state(bes_ctx* ctx, double* U) {
   if (!ctx || !U) return BES_ERR_INVALID;
   const int64_t nc = ctx->soa.nc, nb = ctx->nb;
-  std::vector<double> soa(5 * nc * nb);
-  BES_CUDA_TRY(ctx, cudaMemcpyAsync(soa.data(), ctx->U[ctx->cur], soa.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  state_to_stage_kernel<<<1024, 256, 0, ctx->stream>>>((int)nc, (int)nb, ctx->new2ref_dev,
+                                                       ctx->U[ctx->cur], ctx->stage);
+  ++ctx->launches;
+  BES_CUDA_TRY(ctx, cudaMemcpyAsync(U, ctx->stage, (size_t)nb * nc * 5 * sizeof(double),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
   BES_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  for (int64_t b = 0; b < nb; ++b)
-    for (int64_t i = 0; i < nc; ++i) {
-      const int64_t c = ctx->soa.cell_new2ref[i];
-      for (int v = 0; v < 5; ++v) U[(b * nc + c) * 5 + v] = soa[(b * 5 + v) * nc + i];
-    }
+  BES_CUDA_TRY(ctx, cudaGetLastError());
   return BES_OK;
 }
 

@@ -163,6 +163,10 @@ struct bes_ctx {
     int64_t host_step = 0;
   };
   std::vector<CondImplicit> cond_imp;  // [nb] when nb > 1
+  // state exchange with the caller: raw copies of [nb][nc][5] (reference numbering) into a
+  // staging array, permuted and transposed on the device
+  double* stage = nullptr;             // [nb][nc][5]
+  int32_t* new2ref_dev = nullptr;      // [nc] device cell -> reference cell
   int* nan_flag = nullptr;  // face index + 1 of a NaN flux (0 none)
   double* pinf_dev = nullptr;     // [6] freestream primitives of the current step
   int64_t* step_dev = nullptr;    // solver step counter read by the explicit graphs

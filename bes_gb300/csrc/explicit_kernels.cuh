@@ -351,6 +351,33 @@ static __global__ void reset_dtmin_kernel(unsigned long long* dtmin) {
   *dtmin = (unsigned long long)__double_as_longlong(1e300);
 }
 
+// State exchange: stage [nb][nc][5] in reference numbering <-> U [nb][5][nc] in the device
+// numbering (new2ref: device cell -> reference cell).
+static __global__ void state_from_stage_kernel(int nc, int nb, const int32_t* __restrict__ new2ref,
+                                               const double* __restrict__ stage,
+                                               double* __restrict__ U) {
+  const int64_t n = (int64_t)nc * nb;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / nc, i = t - b * nc;
+    const double* src = stage + (b * nc + new2ref[i]) * 5;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) U[(b * 5 + v) * nc + i] = src[v];
+  }
+}
+static __global__ void state_to_stage_kernel(int nc, int nb, const int32_t* __restrict__ new2ref,
+                                             const double* __restrict__ U,
+                                             double* __restrict__ stage) {
+  const int64_t n = (int64_t)nc * nb;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / nc, i = t - b * nc;
+    double* dst = stage + (b * nc + new2ref[i]) * 5;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dst[v] = U[(b * 5 + v) * nc + i];
+  }
+}
+
 // First node of an explicit iteration (one block): every condition's freestream of this step
 // and global-time-step reset, then the step counter and the history row.
 static __global__ void freestream_step_kernel(Params prm, int nb, int64_t* step, double* pinf_dev,
