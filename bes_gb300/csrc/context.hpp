@@ -88,12 +88,6 @@ struct ImplicitBuffers {
   cudaGraphExec_t factor_graph = nullptr;  // ILU factorisation, all stages
   cudaGraphExec_t apply_graph = nullptr;   // ILU forward+backward sweep, in place on Z
   bool use_colour_ranges = false;          // colour order on contiguous colour ranges
-  // packed copy of the factors' off-diagonal blocks for the colour sweeps: per cell its lower
-  // neighbours first, then its upper ones, each group in local-face order
-  void* P = nullptr;            // [4][25][nc], value type of the system
-  int32_t* padj = nullptr;      // [4][nc] neighbour of packed slot k (-1: none)
-  int8_t* pslot = nullptr;      // [4][nc] local face of packed slot k (-1: none)
-  uint8_t* nlow = nullptr;      // [nc] number of lower neighbours
   std::vector<cudaGraphExec_t> colour_graphs;  // sweeps from V_0..V_m, then from W, into Z
   double cfl_actual = 0;
   double maxres[5] = {0, 0, 0, 0, 0};

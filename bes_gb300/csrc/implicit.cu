@@ -115,8 +115,6 @@ void enqueue_ilu_factor(const Sys<T>& S) {
     ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
                                                         n, c->imp.ilu_pos, S.LU, S.Dinv);
   }
-  if (c->imp.use_colour_ranges)
-    ilu_pack_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, c->imp.pslot, S.LU, (T*)c->imp.P);
 }
 
 // Colour-range sweeps (ilu_colour_kernel) from `in` into S.Z: colours 1..C-2 forward, the last
@@ -125,24 +123,22 @@ template <class T>
 void enqueue_ilu_colour_sweeps(const Sys<T>& S, const T* in) {
   bes_ctx* c = S.c;
   const SoaMesh& M = c->soa;
-  const ImplicitBuffers& I = c->imp;
-  const T* P = (const T*)I.P;
   const int C = M.n_stages;
   const int s1 = M.stage_off[1];
   auto range = [&](int k, int& r0, int& r1) { r0 = M.stage_off[k]; r1 = M.stage_off[k + 1]; };
   int r0, r1;
   for (int k = 1; k < C - 1; ++k) {
     range(k, r0, r1);
-    ilu_colour_packed_kernel<T, true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-        c->dm, r0, r1, s1, P, I.padj, I.nlow, S.Dinv, in, S.Z);
+    ilu_colour_kernel<T, true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
+        c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
   }
   range(C - 1, r0, r1);
-  ilu_colour_packed_kernel<T, true, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-      c->dm, r0, r1, s1, P, I.padj, I.nlow, S.Dinv, in, S.Z);
+  ilu_colour_kernel<T, true, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(c->dm, r0, r1, s1, S.LU,
+                                                                       S.Dinv, in, S.Z);
   for (int k = C - 2; k >= 0; --k) {
     range(k, r0, r1);
-    ilu_colour_packed_kernel<T, false, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-        c->dm, r0, r1, s1, P, I.padj, I.nlow, S.Dinv, in, S.Z);
+    ilu_colour_kernel<T, false, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
+        c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
   }
 }
 
@@ -572,34 +568,6 @@ int implicit_allocate(bes_ctx* c) {
   }
   if (o.linear_solver == 2) build_ilu_schedule(c->soa, true);
   I.use_colour_ranges = o.linear_solver == 1 && colour_ranges(c->soa);
-  if (I.use_colour_ranges) {
-    // packed neighbour order of the colour sweeps: lower neighbours (smaller cell number, an
-    // earlier colour) first, then upper ones, each in local-face order
-    std::vector<int32_t> padj(4 * nc, -1);
-    std::vector<int8_t> pslot(4 * nc, -1);
-    std::vector<uint8_t> nlow(nc, 0);
-    for (int64_t i = 0; i < nc; ++i) {
-      int k = 0;
-      for (int pass = 0; pass < 2; ++pass)
-        for (int s = 0; s < 4; ++s) {
-          const int32_t j = M.adj[s * nc + i];
-          if (j < 0 || (pass == 0) != (j < i)) continue;
-          padj[k * nc + i] = j;
-          pslot[k * nc + i] = (int8_t)s;
-          ++k;
-          if (pass == 0) ++nlow[i];
-        }
-    }
-    rc |= imp_malloc(c, &I.P, 100 * nc * I.tsize);
-    rc |= imp_malloc(c, (void**)&I.padj, 4 * nc * sizeof(int32_t));
-    rc |= imp_malloc(c, (void**)&I.pslot, 4 * nc);
-    rc |= imp_malloc(c, (void**)&I.nlow, nc);
-    if (!rc) {
-      IMP_TRY(c, cudaMemcpy(I.padj, padj.data(), 4 * nc * sizeof(int32_t), cudaMemcpyHostToDevice));
-      IMP_TRY(c, cudaMemcpy(I.pslot, pslot.data(), 4 * nc, cudaMemcpyHostToDevice));
-      IMP_TRY(c, cudaMemcpy(I.nlow, nlow.data(), nc, cudaMemcpyHostToDevice));
-    }
-  }
   if (uses_ilu(c)) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
   rc |= imp_malloc(c, &I.b, N * I.tsize);

@@ -398,34 +398,13 @@ __global__ void __launch_bounds__(128) ilu_upper_kernel(DevMesh m, const int32_t
 //   LOWER only        colours 1..C-2 of the forward sweep: out_i = in_i - sum L_ij y_j
 //   LOWER and UPPER   the last colour: both solves at once (it has no upper neighbours)
 //   UPPER only        colours C-2..0 of the backward sweep: out_i = inv(U_ii)(y_i - sum U_ik z_k)
-// `in` and `out` must not alias.  (ilu_colour_packed_kernel below.)
-
-// Copy the factors' off-diagonal blocks into the packed order (after each factorisation).
-template <class T>
-__global__ void __launch_bounds__(256) ilu_pack_kernel(int nc, const int8_t* __restrict__ pslot,
-                                                       const T* __restrict__ LU, T* __restrict__ P) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nc) return;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int s = pslot[k * nc + i];
-    if (s < 0) continue;
-#pragma unroll
-    for (int q = 0; q < 25; ++q)
-      P[(int64_t)(k * 25 + q) * nc + i] = LU[(int64_t)((1 + s) * 25 + q) * nc + i];
-  }
-}
-
-// The colour sweep reads the packed blocks: the forward sweep packed slots 0..nlow-1, the
-// backward sweep slots nlow..3, so the block loads of a warp use whole sectors (with the
-// local-face slots, a row's lower and upper blocks are interleaved and a warp's loads of one
-// slot fetch every sector while using about half of it).  Lower and upper neighbours each
-// keep their local-face order, so the arithmetic is that of the local-face sweep.
+// `in` and `out` must not alias.
 template <class T, bool LOWER, bool UPPER>
-__global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
-    DevMesh m, int r0, int r1, int s1, const T* __restrict__ P, const int32_t* __restrict__ padj,
-    const uint8_t* __restrict__ nlow, const T* __restrict__ Dinv, const T* __restrict__ in,
-    T* __restrict__ out) {
+__global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int r1, int s1,
+                                                         const T* __restrict__ A,
+                                                         const T* __restrict__ Dinv,
+                                                         const T* __restrict__ in,
+                                                         T* __restrict__ out) {
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1) return;
   const int nc = m.nc;
@@ -433,20 +412,20 @@ __global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
   T acc[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
-  const int nl = nlow[i];
-  const int k0 = LOWER ? 0 : nl;
-  const int k1 = UPPER ? 4 : nl;
-  for (int k = k0; k < k1; ++k) {
-    const int j = padj[k * nc + i];
-    if (j < 0) break;
-    const T* src = (k < nl && j < s1) ? in : out;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int j = m.adj[s * nc + i];
+    const bool lower = LOWER && j >= 0 && j < r0;
+    const bool upper = UPPER && j >= r1;
+    if (!lower && !upper) continue;
+    const T* src = (lower && j < s1) ? in : out;
     T y[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) y[v] = src[(int64_t)j * 5 + v];
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
-      for (int c = 0; c < 5; ++c) acc[r] -= P[(int64_t)(k * 25 + r * 5 + c) * nc + i] * y[c];
+      for (int c = 0; c < 5; ++c) acc[r] -= ellc(A, 1 + s, r * 5 + c, nc, i) * y[c];
   }
   if (UPPER) {
 #pragma unroll
