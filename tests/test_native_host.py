@@ -92,14 +92,17 @@ def _pages_per_warp(new2ref, own, nb):
 
 
 def test_renumbering_keeps_neighbours_close():
-    """Cells are numbered colour by colour, each colour in reverse Cuthill-McKee order: the
-    neighbours of a warp of consecutive cells stay in a few pages, unlike a random order."""
+    """Cells are numbered colour by colour, each colour grouped by its cells' lower-neighbour
+    pattern and in reverse Cuthill-McKee order inside a group: the neighbours of a warp of
+    consecutive cells stay in far fewer pages than in a random order.  (The pattern groups
+    cost some locality, 0.43x of random here against under 0.25x for plain colour-major RCM; the
+    block-ILU(0) sweeps gain 22 % from them and the explicit kernels measured unchanged.)"""
     m = meshgen.bump_channel(30, 10, 8, 0.04)
     g = lib.host_geometry(m)
     own, nb = g["face_owner"], g["face_neigh"]
     new = _pages_per_warp(g["cell_new2ref"], own, nb)
     rnd = _pages_per_warp(np.random.default_rng(0).permutation(len(g["cell_new2ref"])), own, nb)
-    assert new < 0.25 * rnd
+    assert new < 0.5 * rnd
 
 
 def test_mesh_errors_are_reported():
