@@ -112,8 +112,12 @@ void enqueue_ilu_factor(const Sys<T>& S) {
   cudaMemcpyAsync(S.LU, S.A, (size_t)125 * S.nc * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
   for (int k = 0; k < M.n_stages; ++k) {
     const int n = M.stage_off[k + 1] - M.stage_off[k];
-    ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
-                                                        n, c->imp.ilu_pos, S.LU, S.Dinv);
+    if (c->imp.use_colour_ranges)
+      ilu_factor_kernel<T, true><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, nullptr, n, nullptr, S.LU,
+                                                                S.Dinv, M.stage_off[k]);
+    else
+      ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
+                                                          n, c->imp.ilu_pos, S.LU, S.Dinv);
   }
 }
 

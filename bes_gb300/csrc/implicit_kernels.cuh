@@ -256,20 +256,23 @@ static __global__ void __launch_bounds__(256) reduce_rows_kernel(const double* _
 
 // Colour-ordered block ILU(0), one colour per launch (rows of one colour are independent).
 // IKJ order: the lower blocks of a row are eliminated in increasing factorisation position.
-template <class T>
+// RANGE: the stage is the contiguous row range [r0, r0 + nrows) and the factorisation
+// position is the cell number (colour-major numbering), so no row list or position lookup.
+template <class T, bool RANGE = false>
 __global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_t* __restrict__ rows,
                                                          int nrows, const int32_t* __restrict__ pos,
-                                                         T* __restrict__ A, T* __restrict__ Dinv) {
+                                                         T* __restrict__ A, T* __restrict__ Dinv,
+                                                         int r0 = 0) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nrows) return;
   const int nc = m.nc;
-  const int i = rows[t];
-  const int pi = pos[i];
+  const int i = RANGE ? r0 + t : rows[t];
+  const int pi = RANGE ? i : pos[i];
   int nbr[4], pn[4];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     nbr[s] = m.adj[s * nc + i];
-    pn[s] = nbr[s] >= 0 ? pos[nbr[s]] : 0x7fffffff;
+    pn[s] = nbr[s] >= 0 ? (RANGE ? nbr[s] : pos[nbr[s]]) : 0x7fffffff;
   }
   // lower slots sorted by position
   int lo[4], nl = 0;
