@@ -184,6 +184,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x: float, dist) -> float:
+    """The largest value of x over the ranks of the process group (x itself on one rank)."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -359,11 +369,7 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
     clocks.start()
     mixed = implicit_leg(args, torch, ctx, args.steps, args.warmup, flush, with_e2e=False)
     clk = clocks.stop()
-    t_max = mixed["ms"]
-    if dist:
-        tt = torch.tensor([t_max], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = max_over_ranks(mixed["ms"], dist)
     value = world * nc * args.steps / (t_max / 1e3)
     # e2e through the C ABI with host buffers (state up, one step, state down), on the same
     # steps: the solve restarts from the freestream and replays the warm-up untimed
@@ -377,10 +383,7 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
         ctx.implicit_steps(1)
         U = ctx.get_state()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        tt = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(e2e_s, dist)
     # the plain FP64 system on the same steps
     o64 = dict(wl["opts"])
     o64["precision"] = 0
@@ -755,11 +758,7 @@ def main():
     if dist:
         dist.barrier()
     dev_ms = float(sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
-    t_max = dev_ms
-    if dist:
-        tt = torch.tensor([dev_ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = max_over_ranks(dev_ms, dist)
     value = world * ncond * nc * args.steps / (t_max / 1e3)
 
     # end to end through the C ABI with host buffers
@@ -770,11 +769,7 @@ def main():
         ctx.explicit_iterations(1)
         U = ctx.get_state()
     e2e_s = time.perf_counter() - t0
-    e2e_max = e2e_s
-    if dist:
-        tt = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_max = float(tt.item())
+    e2e_max = max_over_ranks(e2e_s, dist)
     e2e = world * ncond * nc * args.steps / e2e_max
 
     n_stage = 4
