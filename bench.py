@@ -82,7 +82,7 @@ WORKLOADS = {
     "sweep_gauss_3m_64": dict(kind="explicit", mesh=("gauss", 100, 50, 100, 1.05),
                               conds=(0, 64),
                               opts=dict(solver_type=0, local_time_step=1, courant_num=0.8)),
-    # learned warm start (scaled form of the survey's configuration 4): 30x15x30-hex Gaussian
+    # learned warm start with the explicit solver: 30x15x30-hex Gaussian
     # box (81,000 tets); training data = the batched explicit solver's states after 1500
     # iterations for 32 conditions (seed 1); 8 held-out conditions (seed 2) run from the
     # network's prediction and from the freestream
@@ -90,7 +90,7 @@ WORKLOADS = {
                                 train=(1, 32), test=(2, 8), data_iters=1500, eval_iters=1500,
                                 train_steps=3000, batch=8192,
                                 opts=dict(solver_type=0, local_time_step=1, courant_num=0.8)),
-    # production form (scaled sweep of the survey's configurations 3-5): 60x30x60-hex Gaussian
+    # warm-started FP32-system implicit sweep against the plain FP64 solver: 60x30x60-hex Gaussian
     # box (648,000 tets); the warm start is trained on 16 conditions (seed 1) solved by a
     # batched FP32-system implicit context; 6 held-out conditions (seed 2) are solved to the
     # same absolute residual (1e-8 of the freestream start's first residual) by the plain FP64

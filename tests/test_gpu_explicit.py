@@ -4,8 +4,8 @@
 Tolerances (floating point, FP64 on both sides; the GPU contracts multiply-adds and uses
 reciprocals where the reference divides):
   operators (dt, gradient, limiter, face states, fluxes): 1e-12 relative to the array's scale;
-  per-iteration residual L2 / max over the first 50 iterations: 1e-10 relative (the bar of the
-  benchmark spec), final state 1e-10.
+  per-iteration residual L2 / max over the first 50 iterations: 1e-10 relative (the parity
+  bar of this path), final state 1e-10.
 """
 import numpy as np
 import pytest
