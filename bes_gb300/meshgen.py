@@ -54,8 +54,14 @@ class TetMesh:
         return int(self.btris.shape[0])
 
     @property
+    def dim(self) -> int:
+        """3 for tetrahedra ([Nc,4], boundary triangles); 2 for triangles ([Nc,3], boundary
+        lines [Nb,2], z = 0)."""
+        return 3 if self.tets.shape[1] == 4 else 2
+
+    @property
     def n_faces(self) -> int:
-        return (4 * self.n_cells + self.n_boundary) // 2
+        return ((self.dim + 1) * self.n_cells + self.n_boundary) // 2
 
 
 def _kuhn_tets() -> np.ndarray:
@@ -139,6 +145,40 @@ def bump_channel(nx: int = 60, ny: int = 20, nz: int = 10, h: float = 0.04) -> T
                    name=f"bump_channel_{nx}x{ny}x{nz}_h{h:g}")
 
 
+def bump_channel_2d(nx: int = 60, ny: int = 20, h: float = 0.04) -> TetMesh:
+    """2-D bump channel: x in [-2, 4], y in [0, 1] over the bump y_b = h cos^2(pi (x - 0.5))
+    for |x - 0.5| < 0.5, nodes mapped y = y_b + eta (1 - y_b); each quad split into two
+    counter-clockwise triangles.  Bottom: slip wall; inflow, outflow and top: freestream."""
+    x = np.linspace(-2.0, 4.0, nx + 1)
+    eta = np.linspace(0.0, 1.0, ny + 1)
+    yb = np.where(np.abs(x - 0.5) < 0.5, h * np.cos(np.pi * (x - 0.5)) ** 2, 0.0)
+    X, E = np.meshgrid(x, eta, indexing="ij")
+    Y = yb[:, None] + E * (1.0 - yb[:, None])
+    nodes = np.stack([X.ravel(), Y.ravel(), np.zeros(X.size)], axis=1)
+
+    def n(i, j):
+        return i * (ny + 1) + j
+
+    tris = []
+    for i in range(nx):
+        for j in range(ny):
+            a, b, c, d = n(i, j), n(i + 1, j), n(i + 1, j + 1), n(i, j + 1)
+            tris += [(a, b, c), (a, c, d)]
+    lines, tags = [], []
+    for i in range(nx):
+        lines.append((n(i, 0), n(i + 1, 0)))
+        tags.append(SLIP_WALL)
+        lines.append((n(i, ny), n(i + 1, ny)))
+        tags.append(FREESTREAM)
+    for j in range(ny):
+        lines.append((n(0, j), n(0, j + 1)))
+        tags.append(FREESTREAM)
+        lines.append((n(nx, j), n(nx, j + 1)))
+        tags.append(FREESTREAM)
+    return TetMesh(nodes, np.array(tris, np.int64), np.array(lines, np.int64),
+                   np.array(tags, np.int64), name=f"bump_channel_2d_{nx}x{ny}_h{h}")
+
+
 def _stretched_symmetric(n: int, half: float, ratio: float) -> np.ndarray:
     """n cells over [-half, half], smallest at 0, sizes growing by ``ratio`` outward."""
     assert n % 2 == 0, "need an even cell count for a grid symmetric about the bump"
@@ -188,15 +228,19 @@ def _fmt_coord(v: float) -> str:
 
 
 def write_gmsh(mesh: TetMesh, path: str) -> None:
-    """Write Gmsh 2.2 ASCII: boundary triangles first, then tets, single spaces, two tags."""
+    """Write Gmsh 2.2 ASCII: boundary faces first (triangles; lines in 2-D), then the cells
+    (tets; triangles in 2-D), single spaces, two tags."""
     nv = mesh.nodes.shape[0]
     nb = mesh.btris.shape[0]
     nc = mesh.tets.shape[0]
+    d = mesh.dim
+    ftype, ctype = (2, 4) if d == 3 else (1, 2)
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
     with open(path, "w") as f:
         f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n")
         f.write("$PhysicalNames\n3\n")
-        f.write(f'2 {SLIP_WALL} "SLIP_WALL"\n2 {FREESTREAM} "FREESTREAM"\n3 {FLUID} "FLUID"\n')
+        f.write(f'{d - 1} {SLIP_WALL} "SLIP_WALL"\n{d - 1} {FREESTREAM} "FREESTREAM"\n'
+                f'{d} {FLUID} "FLUID"\n')
         f.write("$EndPhysicalNames\n")
         f.write(f"$Nodes\n{nv}\n")
         lines = []
@@ -215,7 +259,7 @@ def write_gmsh(mesh: TetMesh, path: str) -> None:
         for i in range(nb):
             t = bt[i]
             tag = int(mesh.btags[i])
-            chunk.append(f"{eid} 2 2 {tag} {tag} {t[0]} {t[1]} {t[2]}\n")
+            chunk.append(f"{eid} {ftype} 2 {tag} {tag} " + " ".join(str(v) for v in t) + "\n")
             eid += 1
             if len(chunk) >= 65536:
                 f.write("".join(chunk))
@@ -223,7 +267,7 @@ def write_gmsh(mesh: TetMesh, path: str) -> None:
         tt = mesh.tets + 1
         for i in range(nc):
             t = tt[i]
-            chunk.append(f"{eid} 4 2 {FLUID} {FLUID} {t[0]} {t[1]} {t[2]} {t[3]}\n")
+            chunk.append(f"{eid} {ctype} 2 {FLUID} {FLUID} " + " ".join(str(v) for v in t) + "\n")
             eid += 1
             if len(chunk) >= 65536:
                 f.write("".join(chunk))

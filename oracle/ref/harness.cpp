@@ -3,6 +3,7 @@
 // that pins the CPU restatement in oracle/ (the reference's ASCII outputs carry ~6 digits).
 //
 //   bes_ref_harness <case.besi> <outdir> <n_steps> [explicit|implicit|kat] [dump_ops] [write]
+//                   [geometry]
 //
 // It builds Config, Mesh, Gas and the solver exactly as main() does (src/BES.cpp:86-108),
 // sets the freestream initial condition, then calls the solver's own timeStep_ n_steps
@@ -14,6 +15,7 @@
 // limiters, per-face MUSCL states and fluxes, first-order flux Jacobians and (implicit) the
 // assembled matrix and right-hand side.  With write it finally calls the reference's
 // Solver::writeToFile_ (solution file in OUTPUT_FORMAT, slip-wall CSV when OUTPUT_SLIP_WALL).
+// With geometry it writes the geometry alone (the operator dumps are 3-D only).
 #include "fluxroe_return_fix.hpp"
 
 #include <cmath>
@@ -39,6 +41,11 @@
 namespace {
 
 std::string g_out;
+// Dimension of the mesh and conserved-variable count.  Every output keeps the 3-D layout
+// ([3] coordinates, [4] local faces, [5] variables); a 2-D mesh's missing entries are zero
+// (face ids -1) and its variables (rho, rho u, rho v, rho E) go to slots 0, 1, 2, 4.
+int g_nd = 3, g_nv = 5;
+inline int slot5(int v) { return (g_nv == 5 || v < 3) ? v : 4; }
 
 void write_bin(const std::string& name, const void* data, size_t bytes) {
   FILE* f = std::fopen((g_out + "/" + name).c_str(), "wb");
@@ -86,20 +93,25 @@ void dump_geometry(Mesh* mesh) {
   for (unsigned long i = 0; i < nc; ++i) {
     Element* e = mesh->getElement(i);
     vol[i] = e->getVolume();
-    for (int d = 0; d < 3; ++d) cen[i * 3 + d] = e->getCentroid()->getSingleCoord(d);
+    for (int d = 0; d < g_nd; ++d) cen[i * 3 + d] = e->getCentroid()->getSingleCoord(d);
     for (int m = 0; m < 4; ++m) {
+      if (m > g_nd) {  // 2-D: three faces per cell
+        cface[i * 4 + m] = -1;
+        cadj[i * 4 + m] = -1;
+        continue;
+      }
       cface[i * 4 + m] = (long long)e->getSingleFace(m)->getId();
       Element* a = e->getFaceAdjacentElement(m);
       cadj[i * 4 + m] = a ? (long long)a->getId() : -1;
       w[i * 4 + m] = e->getFaceInverseDistanceWeight(m);
-      for (int d = 0; d < 3; ++d) r[i * 12 + m * 3 + d] = e->getVectorToFace(m)[d];
+      for (int d = 0; d < g_nd; ++d) r[i * 12 + m * 3 + d] = e->getVectorToFace(m)[d];
     }
   }
   std::vector<double> S(nf * 3), n(nf * 3), area(nf), fc(nf * 3);
   std::vector<long long> own(nf), nei(nf), typ(nf);
   for (unsigned long f = 0; f < nf; ++f) {
     Face* F = mesh->getFace(f);
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < g_nd; ++d) {
       S[f * 3 + d] = F->getDimNormal()[d];
       n[f * 3 + d] = F->getNonDimNormal()[d];
       fc[f * 3 + d] = F->getCenter()->getSingleCoord(d);
@@ -132,10 +144,10 @@ void dump_muscl_face_slots(Mesh* mesh) {
   std::vector<long long> slot(nc * 4, -1);
   for (unsigned long i = 0; i < nc; ++i) {
     Element* e = mesh->getElement(i);
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m <= g_nd; ++m) {
       const unsigned long fid = e->getSingleFace(m)->getId();
       const double* v = e->getVectorToFaceFromFaceId(fid);
-      for (int k = 0; k < 4; ++k)
+      for (int k = 0; k <= g_nd; ++k)
         if (v == e->getVectorToFace(k)) slot[i * 4 + m] = k;
     }
   }
@@ -143,16 +155,25 @@ void dump_muscl_face_slots(Mesh* mesh) {
 }
 
 void norms_of(double** R, unsigned long nc, double* out10) {
-  for (int v = 0; v < 5; ++v) {
+  for (int k = 0; k < 10; ++k) out10[k] = 0.0;
+  for (int v = 0; v < g_nv; ++v) {
     double s = 0.0, mx = 0.0;
     for (unsigned long i = 0; i < nc; ++i) {
       const double a = R[i][v];
       s += a * a;
       mx = std::fabs(a) > mx ? std::fabs(a) : mx;
     }
-    out10[v] = std::sqrt(s);
-    out10[5 + v] = mx;
+    out10[slot5(v)] = std::sqrt(s);
+    out10[5 + slot5(v)] = mx;
   }
+}
+
+// state of a snapshot in the 3-D layout [nc][5]
+std::vector<double> state_of(SolutionSnapshot* s, unsigned long nc) {
+  std::vector<double> U(nc * 5, 0.0);
+  for (unsigned long i = 0; i < nc; ++i)
+    for (int v = 0; v < g_nv; ++v) U[i * 5 + slot5(v)] = s->getConservedVariable(i, (short)v);
+  return U;
 }
 
 }  // namespace
@@ -166,9 +187,10 @@ int main(int argc, char** argv) {
   const std::string besi = argv[1];
   g_out = argv[2];
   const unsigned long nsteps = std::strtoul(argv[3], nullptr, 10);
-  bool dump_ops = false, write_out = false;
+  bool dump_ops = false, write_out = false, dump_geo = false;
   for (int a = 5; a < argc; ++a) {
     dump_ops |= std::string(argv[a]) == "dump_ops";
+    dump_geo |= std::string(argv[a]) == "geometry";
     write_out |= std::string(argv[a]) == "write";
   }
 
@@ -180,6 +202,12 @@ int main(int argc, char** argv) {
   config->initializePostMesh(mesh);
   gas->initialize(config);
   const unsigned long nc = mesh->getNumElement(), nf = mesh->getNumFace();
+  g_nd = mesh->getNumDim();
+  g_nv = config->getNumConservedVariable();
+  if (g_nd != 3 && (dump_ops || (argc > 4 && std::string(argv[4]) == "kat"))) {
+    std::fprintf(stderr, "operator dumps and known-answer records are 3-D only\n");
+    return 2;
+  }
   if (argc > 4 && std::string(argv[4]) == "kat") {
     // Known-answer mode: n records of (UL[5], UR[5], nhat[3]) from outdir/kat_in.bin through
     // the reference's flux and flux-Jacobian objects.  Output per record: Roe F[5], JL[25],
@@ -221,7 +249,7 @@ int main(int argc, char** argv) {
     write_vec("kat_out.bin", out);
     std::_Exit(0);
   }
-  if (dump_ops) dump_geometry(mesh);
+  if (dump_ops || dump_geo) dump_geometry(mesh);
 
   if (config->getSolverType() == SolverType::EXPLICIT) {
     HarnessExplicit* solver = new HarnessExplicit();
@@ -293,12 +321,8 @@ int main(int argc, char** argv) {
     // the reference's own writers, called as its solve loop does after the last step
     // (src/SolverExplicit.cpp:427-433): solution_<n>.vtk|csv and slip_wall_<n>.csv
     if (write_out) solver->writeToFile_(nsteps - 1, config->getNumCurrentSolution() - 1);
-    SolutionSnapshot* s = solver->solution()->getCurrentSnapshot(nsteps, 0);
-    std::vector<double> U(nc * 5);
-    for (unsigned long i = 0; i < nc; ++i)
-      for (int v = 0; v < 5; ++v) U[i * 5 + v] = s->getConservedVariable(i, (short)v);
-    write_vec("final_state.bin", U);
-    if (dump_ops) dump_muscl_face_slots(mesh);
+    write_vec("final_state.bin", state_of(solver->solution()->getCurrentSnapshot(nsteps, 0), nc));
+    if (dump_ops || dump_geo) dump_muscl_face_slots(mesh);
   } else {
     SolverImplicit* solver = new SolverImplicit();
     solver->initialize(config, gas, mesh);
@@ -307,11 +331,15 @@ int main(int argc, char** argv) {
     for (unsigned long it = 0; it < nsteps; ++it) {
       const double cfl_used = solver->actualCourantNum_;
       solver->timeStep_(it, solver->faceLoopVariables_, g_out + "/ref_residual.csv");
-      double l2[5] = {0, 0, 0, 0, 0};
+      double l2[5] = {0, 0, 0, 0, 0}, mx[5] = {0, 0, 0, 0, 0};
       for (unsigned long i = 0; i < nc; ++i)
-        for (int v = 0; v < 5; ++v) l2[v] += solver->explicitFlux_[i * 5 + v] * solver->explicitFlux_[i * 5 + v];
+        for (int v = 0; v < g_nv; ++v) {
+          const double x = solver->explicitFlux_[i * g_nv + v];
+          l2[slot5(v)] += x * x;
+        }
+      for (int v = 0; v < g_nv; ++v) mx[slot5(v)] = solver->maxResidual_[v];
       for (int v = 0; v < 5; ++v) hist.push_back(std::sqrt(l2[v]));
-      for (int v = 0; v < 5; ++v) hist.push_back(solver->maxResidual_[v]);
+      for (int v = 0; v < 5; ++v) hist.push_back(mx[v]);
       hist.push_back(cfl_used);
       hist.push_back(solver->actualCourantNum_);
       if (dump_ops && it == 0) {
@@ -329,12 +357,8 @@ int main(int argc, char** argv) {
     }
     write_vec("implicit_history.bin", hist);
     if (write_out) solver->writeToFile_(nsteps - 1, config->getNumCurrentSolution() - 1);
-    SolutionSnapshot* s = solver->solution_->getCurrentSnapshot(nsteps, 0);
-    std::vector<double> U(nc * 5);
-    for (unsigned long i = 0; i < nc; ++i)
-      for (int v = 0; v < 5; ++v) U[i * 5 + v] = s->getConservedVariable(i, (short)v);
-    write_vec("final_state.bin", U);
-    if (dump_ops) dump_muscl_face_slots(mesh);
+    write_vec("final_state.bin", state_of(solver->solution_->getCurrentSnapshot(nsteps, 0), nc));
+    if (dump_ops || dump_geo) dump_muscl_face_slots(mesh);
   }
   std::fflush(stdout);
   // The reference's destructors loop with 16-bit counters over cells
