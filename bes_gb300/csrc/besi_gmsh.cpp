@@ -9,7 +9,8 @@
 // bes_mesh_read_gmsh follows Mesh::readGmsh (src/Mesh.cpp:95-558): node ids are ignored and
 // nodes are numbered in file order; element node references are 1-based; triangles (type 2)
 // are boundary faces whose first tag names a physical group SLIP_WALL or FREESTREAM;
-// tetrahedra (type 4) are cells; other element types are skipped.
+// tetrahedra (type 4) are cells; other element types are skipped.  When the largest physical
+// name dimension is 2 (2-D), lines (type 1) are the boundary faces and triangles the cells.
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -252,6 +253,7 @@ extern "C" int bes_mesh_read_gmsh(const char* path, bes_mesh_arrays* out, char* 
   std::vector<int32_t> btags;
   std::string line;
   bool tet_seen = false;
+  int nd = 0;  // largest physical-name dimension (Mesh::readGmsh's nDim_)
   while (next_line(line)) {
     if (line == "$PhysicalNames") {
       if (!next_line(line)) break;
@@ -260,6 +262,7 @@ extern "C" int bes_mesh_read_gmsh(const char* path, bes_mesh_arrays* out, char* 
         int dim = 0, tag = 0;
         char name[256] = {0};
         if (std::sscanf(line.c_str(), "%d %d \"%255[^\"]\"", &dim, &tag, name) >= 2) {
+          nd = dim > nd ? dim : nd;
           const std::string nm(name);
           tag_kind[tag] = nm == "SLIP_WALL" ? 1 : (nm == "FREESTREAM" ? 2 : 0);
         }
@@ -288,7 +291,30 @@ extern "C" int bes_mesh_read_gmsh(const char* path, bes_mesh_arrays* out, char* 
           const long v = std::strtol(q, &q, 10);
           if (t == 0) tag0 = v;
         }
-        if (type == 2) {
+        const bool two_d = nd == 2;
+        if (two_d && type == 1) {
+          if (tet_seen) {
+            set_err(err, err_cap,
+                    "boundary line listed after a triangle (the reference's reader needs "
+                    "boundary lines first)");
+            return BES_ERR_MESH;
+          }
+          for (int k = 0; k < 2; ++k) btris.push_back(std::strtoll(q, &q, 10) - 1);
+          auto it = tag_kind.find((int)tag0);
+          const int kind = it == tag_kind.end() ? 0 : it->second;
+          if (kind == 0) {
+            set_err(err, err_cap, "Unknown boundary type entered (physical tag " +
+                                      std::to_string(tag0) + ")");
+            return BES_ERR_MESH;
+          }
+          btags.push_back(kind);
+        } else if (two_d && type == 2) {
+          tet_seen = true;
+          for (int k = 0; k < 3; ++k) tets.push_back(std::strtoll(q, &q, 10) - 1);
+        } else if (two_d && type == 4) {
+          set_err(err, err_cap, "tetrahedron in a 2D problem");
+          return BES_ERR_MESH;
+        } else if (type == 2) {
           if (tet_seen) {
             set_err(err, err_cap,
                     "boundary triangle listed after a tetrahedron (the reference's reader needs "
@@ -317,9 +343,10 @@ extern "C" int bes_mesh_read_gmsh(const char* path, bes_mesh_arrays* out, char* 
     }
   }
   if (nodes.empty() || tets.empty()) {
-    set_err(err, err_cap, "mesh has no nodes or no tetrahedra");
+    set_err(err, err_cap, "mesh has no nodes or no cells");
     return BES_ERR_MESH;
   }
+  const int nvc = nd == 2 ? 3 : 4;
   double* X = (double*)std::malloc(nodes.size() * sizeof(double));
   int64_t* T = (int64_t*)std::malloc(tets.size() * sizeof(int64_t));
   int64_t* B = (int64_t*)std::malloc((btris.size() + 1) * sizeof(int64_t));
@@ -330,8 +357,9 @@ extern "C" int bes_mesh_read_gmsh(const char* path, bes_mesh_arrays* out, char* 
   if (!btags.empty()) std::memcpy(BT, btags.data(), btags.size() * sizeof(int32_t));
   out->n_nodes = (int64_t)nodes.size() / 3;
   out->nodes = X;
-  out->n_tets = (int64_t)tets.size() / 4;
+  out->n_tets = (int64_t)tets.size() / nvc;
   out->tets = T;
+  out->dim = nd == 2 ? 2 : 3;
   out->n_btris = (int64_t)btags.size();
   out->btris = B;
   out->btags = BT;
@@ -403,7 +431,8 @@ extern "C" int bes_host_geometry(const bes_mesh_arrays* mesh, int32_t muscl_face
   bes::RefMesh M;
   std::string e;
   if (!bes::build_ref_mesh(mesh->nodes, mesh->n_nodes, mesh->btris, mesh->btags, mesh->n_btris,
-                           mesh->tets, mesh->n_tets, muscl_face_vector != 0, M, e)) {
+                           mesh->tets, mesh->n_tets, bes_mesh_dim(mesh), muscl_face_vector != 0,
+                           M, e)) {
     set_err(err, err_cap, e);
     return BES_ERR_MESH;
   }

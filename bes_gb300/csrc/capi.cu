@@ -200,12 +200,13 @@ int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_co
   cudaGetDevice(&ctx->device);
   std::string err;
   if (!build_ref_mesh(mesh->nodes, mesh->n_nodes, mesh->btris, mesh->btags, mesh->n_btris,
-                      mesh->tets, mesh->n_tets, opt->muscl_face_vector != 0, ctx->ref, err)) {
+                      mesh->tets, mesh->n_tets, bes_mesh_dim(mesh), opt->muscl_face_vector != 0,
+                      ctx->ref, err)) {
     return BES_ERR_MESH;
   }
   build_soa(ctx->ref, opt->venkatakrishnan_factor, opt->muscl_face_vector != 0, true, ctx->soa);
   ctx->nodes.assign(mesh->nodes, mesh->nodes + mesh->n_nodes * 3);
-  ctx->tets.assign(mesh->tets, mesh->tets + mesh->n_tets * 4);
+  ctx->tets.assign(mesh->tets, mesh->tets + mesh->n_tets * (bes_mesh_dim(mesh) + 1));
   const SoaMesh& S = ctx->soa;
   bes_ctx* c = ctx.get();
   BES_CUDA_TRY(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -270,10 +271,12 @@ int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_co
   // gas and freestream (Config::initializePostMesh, src/Config.cpp:480-488), per condition
   c->prm.gas = make_gas(opt->gas_constant, opt->specific_heat_ratio, opt->harten_correction_limit);
   c->pinf0_host.assign(6 * nb, 0.0);
+  const int S_dim = c->ref.dim;
   for (int64_t b = 0; b < nb; ++b) {
     double* p = &c->pinf0_host[6 * b];
     p[0] = 1.0;
-    for (int d = 0; d < 3; ++d) p[1 + d] = mach[3 * b + d];
+    // a 2-D mesh reads the first two FREESTREAM_MACH components (velocity w stays 0)
+    for (int d = 0; d < S_dim; ++d) p[1 + d] = mach[3 * b + d];
     p[4] = 1.0 / opt->specific_heat_ratio;
     p[5] = 1.0 / (opt->specific_heat_ratio * opt->gas_constant);
   }

@@ -280,6 +280,7 @@ __global__ void __launch_bounds__(kBlock) update_kernel(
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int g = m.gface[q * nc + c];
+      if (g == bes::kNoFace) continue;  // empty slot of a triangle
       const int f = g >= 0 ? g : ~g;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {

@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(128) cell_assemble_kernel(
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       const int gf = m.gface[s * nc + i];
+      if (gf == bes::kNoFace) continue;  // empty slot of a triangle
       const int f = gf >= 0 ? gf : ~gf;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {

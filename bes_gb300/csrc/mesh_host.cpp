@@ -95,14 +95,186 @@ inline void sort3(int64_t* k) {
   if (k[0] > k[1]) std::swap(k[0], k[1]);
 }
 
+// Per-cell data that follows from the faces, for cells with `nfc` faces (slots nfc..3 empty):
+// neighbours, inverse-distance weights (Element::computeAllFaceInverseDistanceWeightage,
+// src/Element.cpp:120-139), projected lengths (TimeStepCalculatorLocal::computeProjectedLength_,
+// src/TimeStepCalculatorLocal.cpp:51-63) and the MUSCL face-vector slot (Q13: the local face
+// map is keyed by face id 0 for every face, so face 0 resolves to the cell's last slot).
+void cell_links(RefMesh& M, int nfc, bool muscl_exact) {
+  const int64_t nc = M.nc;
+  for (int64_t c = 0; c < nc; ++c) {
+    for (int m = 0; m < nfc; ++m) {
+      const int64_t f = M.cface[c * 4 + m];
+      if (M.kind[f] == KIND_INTERNAL) M.cadj[c * 4 + m] = (M.owner[f] != c) ? M.owner[f] : M.neigh[f];
+    }
+    for (int m = 0; m < nfc; ++m) {
+      const int64_t a = M.cadj[c * 4 + m];
+      if (a < 0) continue;
+      const int64_t f = M.cface[c * 4 + m];
+      double d1 = 0, d2 = 0;
+      for (int d = 0; d < 3; ++d) {
+        const double x1 = M.centroid[c * 3 + d] - M.center[f * 3 + d];
+        const double x2 = M.centroid[a * 3 + d] - M.center[f * 3 + d];
+        d1 += x1 * x1;
+        d2 += x2 * x2;
+      }
+      d1 = std::sqrt(d1);
+      d2 = std::sqrt(d2);
+      M.weight[c * 4 + m] = d2 / (d1 + d2);
+    }
+    for (int m = 0; m < nfc; ++m)
+      for (int d = 0; d < 3; ++d) M.plen[c * 3 + d] += std::fabs(M.S[M.cface[c * 4 + m] * 3 + d]);
+    for (int d = 0; d < 3; ++d) M.plen[c * 3 + d] /= 2.0;
+    for (int m = 0; m < nfc; ++m)
+      M.muscl_slot[c * 4 + m] =
+          (int8_t)(muscl_exact ? m : (M.cface[c * 4 + m] == 0 ? nfc - 1 : 0));
+  }
+}
+
+// Triangle meshes (Mesh::readGmsh, src/Mesh.cpp:235-426; MeshGmsh.cpp:22-42, 71-93): boundary
+// lines first in file order with normal (y1 - y0, x0 - x1); a triangle's edges are
+// (v0,v1), (v1,v2), (v2,v0), a new edge takes that order (normal out of the triangle that
+// creates it), and a boundary line is flipped when it opposes the triangle's outward normal
+// (y_b - y_a, x_a - x_b) (MeshMath::computeTwoDimOutwardNormal, src/MeshCommon.cpp:60-67).
+// Area 0.5 |(x0 - x1)(y2 - y1) - (x2 - x1)(y0 - y1)|, centroid (v0 + v1 + v2)/3.  Only x and y
+// are read; z of every centre and normal is 0, and face slot 3 of every cell stays empty.
+bool build_ref_mesh_2d(const double* X, int64_t nv, const int64_t* blines, const int32_t* btags,
+                       int64_t nb, const int64_t* tris, int64_t nc, bool muscl_exact, RefMesh& M,
+                       std::string& err) {
+  M.dim = 2;
+  const int64_t nf_est = (3 * nc + nb) / 2 + 16;
+  M.S.reserve(nf_est * 3);
+  M.nhat.reserve(nf_est * 3);
+  M.center.reserve(nf_est * 3);
+  M.area.reserve(nf_est);
+  M.owner.reserve(nf_est);
+  M.neigh.reserve(nf_est);
+  M.kind.reserve(nf_est);
+  FaceTable table((size_t)nf_est);
+  auto new_face = [&](int64_t v0, int64_t v1, int8_t kind) -> int64_t {
+    const int64_t id = (int64_t)M.kind.size();
+    const double* a = &X[v0 * 3];
+    const double* b = &X[v1 * 3];
+    const double S[2] = {b[1] - a[1], a[0] - b[0]};
+    const double area = std::sqrt(S[0] * S[0] + S[1] * S[1]);
+    for (int d = 0; d < 2; ++d) {
+      M.S.push_back(S[d]);
+      M.nhat.push_back(S[d] / area);
+      M.center.push_back(0.5 * (a[d] + b[d]));
+    }
+    M.S.push_back(0.0);
+    M.nhat.push_back(0.0);
+    M.center.push_back(0.0);
+    M.area.push_back(area);
+    M.owner.push_back(-1);
+    M.neigh.push_back(-1);
+    M.kind.push_back(kind);
+    return id;
+  };
+  for (int64_t b = 0; b < nb; ++b) {
+    const int64_t* v = &blines[b * 2];
+    for (int q = 0; q < 2; ++q)
+      if (v[q] < 0 || v[q] >= nv) {
+        err = "boundary line references a missing node";
+        return false;
+      }
+    int8_t kind;
+    if (btags[b] == 1)
+      kind = KIND_SLIP_WALL;
+    else if (btags[b] == 2)
+      kind = KIND_FREESTREAM;
+    else {
+      err = "boundary line with an unknown boundary tag " + std::to_string(btags[b]);
+      return false;
+    }
+    int64_t k[3] = {std::min(v[0], v[1]), std::max(v[0], v[1]), -2};
+    table.overwrite(k, new_face(v[0], v[1], kind));
+  }
+  M.nc = nc;
+  M.cface.assign(nc * 4, -1);
+  M.cadj.assign(nc * 4, -1);
+  for (int64_t c = 0; c < nc; ++c) {
+    const int64_t* p = &tris[c * 3];
+    for (int q = 0; q < 3; ++q)
+      if (p[q] < 0 || p[q] >= nv) {
+        err = "triangle references a missing node";
+        return false;
+      }
+    for (int m = 0; m < 3; ++m) {
+      const int64_t va = p[m], vb = p[(m + 1) % 3];
+      int64_t k[3] = {std::min(va, vb), std::max(va, vb), -2};
+      const int64_t next = (int64_t)M.kind.size();
+      int64_t f = table.find_or_insert(k, next);
+      if (f < 0) {
+        f = new_face(va, vb, KIND_INTERNAL);
+        M.owner[f] = c;
+      } else if (M.kind[f] != KIND_INTERNAL) {
+        const double out[2] = {X[vb * 3 + 1] - X[va * 3 + 1], -X[vb * 3] + X[va * 3]};
+        const double dp = M.S[f * 3] * out[0] + M.S[f * 3 + 1] * out[1];
+        if (dp < 0)
+          for (int d = 0; d < 2; ++d) {
+            M.S[f * 3 + d] = -M.S[f * 3 + d];
+            M.nhat[f * 3 + d] = -M.nhat[f * 3 + d];
+          }
+        M.owner[f] = c;
+        M.neigh[f] = -1;
+      } else {
+        if (M.neigh[f] >= 0) {
+          err = "an edge is shared by more than two triangles";
+          return false;
+        }
+        M.neigh[f] = c;
+      }
+      M.cface[c * 4 + m] = f;
+    }
+  }
+  M.nf = (int64_t)M.kind.size();
+  for (int64_t f = 0; f < M.nf; ++f) {
+    if (M.owner[f] < 0) {
+      err = "boundary line " + std::to_string(f) + " is not an edge of any triangle";
+      return false;
+    }
+    if (M.kind[f] == KIND_INTERNAL && M.neigh[f] < 0) {
+      err = "edge " + std::to_string(f) +
+            " belongs to one triangle only and no boundary line covers it";
+      return false;
+    }
+  }
+  M.vol.assign(nc, 0);
+  M.centroid.assign(nc * 3, 0);
+  M.rvec.assign(nc * 12, 0);
+  M.weight.assign(nc * 4, 0);
+  M.plen.assign(nc * 3, 0);
+  M.muscl_slot.assign(nc * 4, 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    const double* x0 = &X[tris[c * 3] * 3];
+    const double* x1 = &X[tris[c * 3 + 1] * 3];
+    const double* x2 = &X[tris[c * 3 + 2] * 3];
+    M.vol[c] = 0.5 * std::fabs((x0[0] - x1[0]) * (x2[1] - x1[1]) - (x2[0] - x1[0]) * (x0[1] - x1[1]));
+    for (int d = 0; d < 2; ++d) M.centroid[c * 3 + d] = (x0[d] + x1[d] + x2[d]) / 3;
+    for (int m = 0; m < 3; ++m) {
+      const int64_t f = M.cface[c * 4 + m];
+      for (int d = 0; d < 2; ++d)
+        M.rvec[c * 12 + m * 3 + d] = M.center[f * 3 + d] - M.centroid[c * 3 + d];
+    }
+  }
+  cell_links(M, 3, muscl_exact);
+  return true;
+}
+
 }  // namespace
 
 bool build_ref_mesh(const double* X, int64_t nv, const int64_t* btris, const int32_t* btags,
-                    int64_t nb, const int64_t* tets, int64_t nc, bool muscl_exact, RefMesh& M,
-                    std::string& err) {
+                    int64_t nb, const int64_t* tets, int64_t nc, int dim, bool muscl_exact,
+                    RefMesh& M, std::string& err) {
   M = RefMesh();
   if (nc <= 0 || nv <= 0) {
     err = "empty mesh";
+    return false;
+  }
+  if (dim == 2) return build_ref_mesh_2d(X, nv, btris, btags, nb, tets, nc, muscl_exact, M, err);
+  if (dim != 3) {
+    err = "mesh dimension must be 2 or 3";
     return false;
   }
   const int64_t nf_est = (4 * nc + nb) / 2 + 16;
@@ -242,32 +414,7 @@ bool build_ref_mesh(const double* X, int64_t nv, const int64_t* btris, const int
         M.rvec[c * 12 + m * 3 + d] = M.center[f * 3 + d] - M.centroid[c * 3 + d];
     }
   }
-  for (int64_t c = 0; c < nc; ++c) {
-    for (int m = 0; m < 4; ++m) {
-      const int64_t f = M.cface[c * 4 + m];
-      if (M.kind[f] == KIND_INTERNAL) M.cadj[c * 4 + m] = (M.owner[f] != c) ? M.owner[f] : M.neigh[f];
-    }
-    for (int m = 0; m < 4; ++m) {
-      const int64_t a = M.cadj[c * 4 + m];
-      if (a < 0) continue;
-      const int64_t f = M.cface[c * 4 + m];
-      double d1 = 0, d2 = 0;
-      for (int d = 0; d < 3; ++d) {
-        const double x1 = M.centroid[c * 3 + d] - M.center[f * 3 + d];
-        const double x2 = M.centroid[a * 3 + d] - M.center[f * 3 + d];
-        d1 += x1 * x1;
-        d2 += x2 * x2;
-      }
-      d1 = std::sqrt(d1);
-      d2 = std::sqrt(d2);
-      M.weight[c * 4 + m] = d2 / (d1 + d2);
-    }
-    for (int m = 0; m < 4; ++m)
-      for (int d = 0; d < 3; ++d) M.plen[c * 3 + d] += std::fabs(M.S[M.cface[c * 4 + m] * 3 + d]);
-    for (int d = 0; d < 3; ++d) M.plen[c * 3 + d] /= 2.0;
-    for (int m = 0; m < 4; ++m)
-      M.muscl_slot[c * 4 + m] = (int8_t)(muscl_exact ? m : (M.cface[c * 4 + m] == 0 ? 3 : 0));
-  }
+  cell_links(M, 4, muscl_exact);
   return true;
 }
 
@@ -482,15 +629,27 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
     S.vol[i] = M.vol[c];
     S.inv_vol[i] = 1.0 / M.vol[c];
     // epsilon of LimiterVenkatakrishnan (src/LimiterVenkatakrishnan.cpp:42-46), squared
-    const double eps = std::pow(venkat_k * std::pow(M.vol[c], 1.0 / 3), 3.0 / 2.0);
+    const double eps = std::pow(venkat_k * std::pow(M.vol[c], 1.0 / M.dim), 3.0 / 2.0);
     S.eps2[i] = eps * eps;
     for (int d = 0; d < 3; ++d) S.plen[d * nc + i] = M.plen[c * 3 + d];
     int order[4] = {0, 1, 2, 3};
-    std::sort(order, order + 4,
-              [&](int a, int b) { return M.cface[c * 4 + a] < M.cface[c * 4 + b]; });
+    // faces in reference-id order, an empty slot last
+    auto key = [&](int m) { return M.cface[c * 4 + m] < 0 ? INT64_MAX : M.cface[c * 4 + m]; };
+    std::sort(order, order + 4, [&](int a, int b) { return key(a) < key(b); });
     for (int m = 0; m < 4; ++m) {
       const int64_t f = M.cface[c * 4 + m];
       const int64_t a = M.cadj[c * 4 + m];
+      if (f < 0) {
+        // empty slot of a triangle: no neighbour, no area, weight 0, no face
+        S.adj[m * nc + i] = -1;
+        S.cface[m * nc + i] = -1;
+        for (int d = 0; d < 3; ++d) {
+          S.Sc[(m * 3 + d) * nc + i] = 0.0;
+          S.r[(m * 3 + d) * nc + i] = 0.0;
+        }
+        S.w[m * nc + i] = 0.0;
+        continue;
+      }
       S.adj[m * nc + i] = a >= 0 ? (int32_t)S.cell_ref2new[a] : -1;
       S.cface[m * nc + i] = (int32_t)S.face_ref2new[f];
       const double sgn = (M.owner[f] == c) ? 1.0 : -1.0;
@@ -500,7 +659,13 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
       }
       S.w[m * nc + i] = M.weight[c * 4 + m];
       if (M.kind[f] == KIND_SLIP_WALL) S.cflags[i] |= (uint8_t)(1u << m);
+    }
+    for (int m = 0; m < 4; ++m) {
       const int64_t fo = M.cface[c * 4 + order[m]];
+      if (fo < 0) {
+        S.gface[m * nc + i] = kNoFace;
+        continue;
+      }
       const int32_t fnew = (int32_t)S.face_ref2new[fo];
       S.gface[m * nc + i] = (M.owner[fo] == c) ? fnew : ~fnew;
     }

@@ -1,17 +1,22 @@
 // Host-side mesh pre-processing: the reference's face discovery and geometry, its quirks, and
 // the GB300 renumbering into structure-of-arrays.
 #pragma once
+#include <climits>
 #include <cstdint>
 #include <string>
 #include <vector>
 
 namespace bes {
 
+// gface entry of an empty face slot (slot 3 of a triangle); never a face id or its complement
+constexpr int32_t kNoFace = INT32_MIN;
+
 enum FaceKind : int8_t { KIND_INTERNAL = 0, KIND_SLIP_WALL = 1, KIND_FREESTREAM = 2 };
 
 // Mesh with the reference's semantics, in reference numbering (src/Mesh.cpp:95-636).
 struct RefMesh {
   int64_t nc = 0, nf = 0;
+  int dim = 3;  // 2: triangles (face slot 3 of every cell is empty: cface = cadj = -1)
   std::vector<double> S, nhat, area, center;  // per face [3], [3], [1], [3]
   std::vector<int64_t> owner, neigh;          // neigh = -1 on boundary faces
   std::vector<int8_t> kind;
@@ -20,10 +25,12 @@ struct RefMesh {
   std::vector<int8_t> muscl_slot;                         // [4] per cell
 };
 
-// Build from Gmsh-ordered arrays.  Returns false with a message on an unusable mesh.
+// Build from Gmsh-ordered arrays: dim 3 takes boundary triangles [nb][3] and tetrahedra
+// [nc][4], dim 2 boundary lines [nb][2] and triangles [nc][3].  Returns false with a message
+// on an unusable mesh.
 bool build_ref_mesh(const double* X, int64_t nv, const int64_t* btris, const int32_t* btags,
-                    int64_t nb, const int64_t* tets, int64_t nc, bool muscl_exact, RefMesh& M,
-                    std::string& err);
+                    int64_t nb, const int64_t* tets, int64_t nc, int dim, bool muscl_exact,
+                    RefMesh& M, std::string& err);
 
 // Device-ready arrays after renumbering (all vectors already in the device layout).
 struct SoaMesh {
@@ -34,7 +41,8 @@ struct SoaMesh {
   // cells: SoA [k][nc]
   std::vector<double> vol, inv_vol, eps2, plen;  // plen [3][nc]
   std::vector<int32_t> adj, cface, gface;        // [4][nc]; gface: faces in reference-id order,
-                                                 // ~f when the cell is the face's neighbour
+                                                 // ~f when the cell is the face's neighbour,
+                                                 // kNoFace in empty slots (triangles)
   std::vector<double> Sc, w, r;                  // [4*3][nc], [4][nc], [4*3][nc]
   std::vector<uint8_t> cflags;                   // bit m: face m is a slip wall; bit 4: has extras
   std::vector<int32_t> extra_cell;               // [n_extra], sorted

@@ -66,27 +66,37 @@ int write_file(const OutMesh& m, const double* U, double gamma, double R, const 
     err = std::string("cannot open ") + path + " for writing";
     return BES_ERR_INVALID;
   }
+  // primitive columns: rho, the nd velocity (Mach) components, p, T
+  const int nd = M.dim;
+  const int nvc = nd + 1;  // vertices per cell
+  int pcols[6], np = 0;
+  pcols[np++] = 0;
+  for (int k = 0; k < nd; ++k) pcols[np++] = 1 + k;
+  pcols[np++] = 4;
+  pcols[np++] = 5;
   if (kind == BES_OUTPUT_CSV) {  // SolutionSnapshot::writePrimitiveToCsv
     for (int64_t i = 0; i < nc; ++i) {
-      for (int k = 0; k < 3; ++k) out << M.centroid[i * 3 + k] << ",";
-      for (int v = 0; v < 6; ++v) out << D[i * 6 + v] << ",";
+      for (int k = 0; k < nd; ++k) out << M.centroid[i * 3 + k] << ",";
+      for (int v = 0; v < np; ++v) out << D[i * 6 + pcols[v]] << ",";
       out << "\n";
     }
   } else if (kind == BES_OUTPUT_VTK) {  // SolutionSnapshot::writePrimitiveToVtk
     out << "# vtk DataFile Version 2.0\n" << path << "\nASCII\nDATASET UNSTRUCTURED_GRID\n";
     out << "POINTS " << m.n_nodes << " float\n";
     for (int64_t v = 0; v < m.n_nodes; ++v) {
-      for (int k = 0; k < 3; ++k) out << m.nodes[v * 3 + k] << " ";
+      for (int k = 0; k < nd; ++k) out << m.nodes[v * 3 + k] << " ";
+      if (nd == 2) out << 0.0 << " ";
       out << "\n";
     }
-    out << "CELLS " << nc << " " << nc * 5 << "\n";
+    out << "CELLS " << nc << " " << nc * (nvc + 1) << "\n";
     for (int64_t i = 0; i < nc; ++i) {
-      out << 4 << " ";
-      for (int k = 0; k < 4; ++k) out << m.tets[i * 4 + k] << " ";
+      out << nvc << " ";
+      for (int k = 0; k < nvc; ++k) out << m.tets[i * nvc + k] << " ";
       out << "\n";
     }
     out << "CELL_TYPES " << nc << "\n";
-    for (int64_t i = 0; i < nc; ++i) out << 10 << "\n";
+    // VTK_TETRA 10 (ElementGmshFour), VTK_TRIANGLE 5 (ElementGmshTwo)
+    for (int64_t i = 0; i < nc; ++i) out << (nd == 3 ? 10 : 5) << "\n";
     out << "CELL_DATA " << nc << "\n";
     const char* names[3] = {"rho_nondim", "P_nondim", "T_nondim"};
     const int cols[3] = {0, 4, 5};
@@ -96,16 +106,17 @@ int write_file(const OutMesh& m, const double* U, double gamma, double R, const 
     }
     out << "VECTORS M double\n";
     for (int64_t i = 0; i < nc; ++i) {
-      for (int k = 0; k < 3; ++k) out << D[i * 6 + 1 + k] << " ";
+      for (int k = 0; k < nd; ++k) out << D[i * 6 + 1 + k] << " ";
+      if (nd == 2) out << 0.0 << " ";
       out << "\n";
     }
   } else if (kind == BES_OUTPUT_SLIP_WALL_CSV) {  // SolutionSnapshot::writeSlipWallToCsv
     for (int64_t f = 0; f < M.nf; ++f) {
       if (M.kind[f] != 1) continue;
       const int64_t o = M.owner[f];
-      for (int k = 0; k < 3; ++k) out << M.center[f * 3 + k] << ",";
-      for (int k = 0; k < 3; ++k) out << M.S[f * 3 + k] << ",";
-      for (int v = 0; v < 6; ++v) out << D[o * 6 + v] << ",";
+      for (int k = 0; k < nd; ++k) out << M.center[f * 3 + k] << ",";
+      for (int k = 0; k < nd; ++k) out << M.S[f * 3 + k] << ",";
+      for (int v = 0; v < np; ++v) out << D[o * 6 + pcols[v]] << ",";
       out << "\n";
     }
   } else {
@@ -139,7 +150,8 @@ int bes_write_host(const bes_mesh_arrays* mesh, const bes_options* opt, const do
   bes::RefMesh M;
   std::string e;
   if (!bes::build_ref_mesh(mesh->nodes, mesh->n_nodes, mesh->btris, mesh->btags, mesh->n_btris,
-                           mesh->tets, mesh->n_tets, opt->muscl_face_vector != 0, M, e)) {
+                           mesh->tets, mesh->n_tets, bes_mesh_dim(mesh),
+                           opt->muscl_face_vector != 0, M, e)) {
     set_err(err, err_cap, e);
     return BES_ERR_MESH;
   }
@@ -174,10 +186,13 @@ int bes_solve(bes_ctx* ctx, const bes_output* out) {
   const std::string folder = out->folder;
   const std::string res_path = folder + "/residual.csv";
   { std::ofstream trunc(res_path); if (!trunc) { ctx->last_error = "cannot open " + res_path; return BES_ERR_INVALID; } }
+  // conserved variables of the mesh dimension: a 2-D mesh has no rho w
+  const int nvar = ctx->ref.dim + 2;
+  const int vars[5] = {0, 1, 2, nvar == 4 ? 4 : 3, 4};
   if (out->verbose) {
     std::cout << "Running solver on the GPU..." << std::endl << std::endl;
     std::cout << "  | Time step | ";
-    for (int v = 0; v < 5; ++v) std::cout << "Conserved variable " << (v + 1) << " | ";
+    for (int v = 0; v < nvar; ++v) std::cout << "Conserved variable " << (v + 1) << " | ";
     std::cout << std::endl;
   }
   const int ncol = implicit ? 19 : 10;
@@ -203,9 +218,9 @@ int bes_solve(bes_ctx* ctx, const bes_output* out) {
       line << (it + q + 1) << ",";
       line << std::scientific;
       con << std::scientific << "  | " << (it + q + 1) << " | ";
-      for (int v = 0; v < 5; ++v) {
-        line << h[5 + v] << ",";
-        con << h[5 + v] << " | ";
+      for (int k = 0; k < nvar; ++k) {
+        line << h[5 + vars[k]] << ",";
+        con << h[5 + vars[k]] << " | ";
       }
       if (implicit) {
         line << (int64_t)h[12] << "," << h[13] << ",";

@@ -47,7 +47,7 @@ class MeshArrays(ctypes.Structure):
     _fields_ = [("n_nodes", ctypes.c_int64), ("nodes", ctypes.POINTER(ctypes.c_double)),
                 ("n_btris", ctypes.c_int64), ("btris", ctypes.POINTER(ctypes.c_int64)),
                 ("btags", ctypes.POINTER(ctypes.c_int32)), ("n_tets", ctypes.c_int64),
-                ("tets", ctypes.POINTER(ctypes.c_int64))]
+                ("tets", ctypes.POINTER(ctypes.c_int64)), ("dim", ctypes.c_int32)]
 
 
 class Output(ctypes.Structure):
@@ -251,7 +251,8 @@ class _MeshKeep:
                             self.btris.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                             self.btags.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                             self.tets.shape[0],
-                            self.tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+                            self.tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                            2 if self.tets.shape[1] == 3 else 3)
 
 
 def _i(a):
@@ -295,13 +296,14 @@ def read_gmsh(path: str):
     if rc != BES_OK:
         raise BesError(rc, err.value.decode())
     try:
+        nd = 2 if m.dim == 2 else 3
         nodes = np.ctypeslib.as_array(m.nodes, shape=(m.n_nodes, 3)).copy()
-        tets = np.ctypeslib.as_array(m.tets, shape=(m.n_tets, 4)).copy()
+        tets = np.ctypeslib.as_array(m.tets, shape=(m.n_tets, nd + 1)).copy()
         if m.n_btris:
-            btris = np.ctypeslib.as_array(m.btris, shape=(m.n_btris, 3)).copy()
+            btris = np.ctypeslib.as_array(m.btris, shape=(m.n_btris, nd)).copy()
             btags = np.ctypeslib.as_array(m.btags, shape=(m.n_btris,)).copy().astype(np.int64)
         else:
-            btris = np.zeros((0, 3), np.int64)
+            btris = np.zeros((0, nd), np.int64)
             btags = np.zeros(0, np.int64)
     finally:
         L.bes_mesh_free(ctypes.byref(m))

@@ -39,17 +39,22 @@ extern "C" {
 #define BES_TAG_SLIP_WALL 1
 #define BES_TAG_FREESTREAM 2
 
-/* Mesh as read from a Gmsh 2.2 file: nodes, the boundary triangles in file order, then the
- * tetrahedra in file order.  All ids 0-based. */
+/* Mesh as read from a Gmsh 2.2 file: nodes, the boundary faces in file order, then the cells
+ * in file order.  All ids 0-based.  3-D (dim 0 or 3): boundary triangles and tetrahedra.
+ * 2-D (dim 2, Mesh::readGmsh's nDim from the physical names, src/Mesh.cpp:170-183): boundary
+ * lines [n_btris][2] and triangles [n_tets][3], counter-clockwise; z is ignored. */
 typedef struct {
   int64_t n_nodes;
   const double* nodes;   /* [n_nodes][3] */
   int64_t n_btris;
-  const int64_t* btris;  /* [n_btris][3] */
+  const int64_t* btris;  /* [n_btris][3] (2-D: [n_btris][2]) */
   const int32_t* btags;  /* [n_btris] BES_TAG_* */
   int64_t n_tets;
-  const int64_t* tets;   /* [n_tets][4] positively oriented */
+  const int64_t* tets;   /* [n_tets][4] positively oriented (2-D: [n_tets][3]) */
+  int32_t dim;           /* 0 or 3: tetrahedra; 2: triangles */
 } bes_mesh_arrays;
+
+static inline int bes_mesh_dim(const bes_mesh_arrays* m) { return m->dim == 2 ? 2 : 3; }
 
 /* Options: the .besi keys of the reference (src/Config.cpp:73-422) plus additive keys. */
 typedef struct {

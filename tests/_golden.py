@@ -12,11 +12,16 @@ MESHES = {
     "bump_channel_12x4x4_h0.04": lambda: meshgen.bump_channel(12, 4, 4, 0.04),
     "bump_channel_12x4x4_h0.08": lambda: meshgen.bump_channel(12, 4, 4, 0.08),
     "gaussian_box_8x4x8_r1.05": lambda: meshgen.gaussian_box(8, 4, 8),
+    "bump_channel_2d_24x8_h0.08": lambda: meshgen.bump_channel_2d(24, 8, 0.08),
 }
 
 CASES = ["explicit_bump_local", "explicit_bump_global", "explicit_gauss_pitch",
          "explicit_bump_supersonic", "explicit_bump_ramp", "implicit_bump_jacobi",
          "implicit_bump_ilu0"]
+
+# triangle meshes (the reference's 2-D path); the fixtures pad per-cell data to the 3-D
+# layout: five conserved variables (rho w = 0) and four face slots (the fourth -1)
+CASES_2D = ["explicit_bump2d_local"]
 
 
 def load(name):

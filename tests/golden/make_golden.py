@@ -75,6 +75,14 @@ OUTPUT_CASES = {
                                  mach=meshgen.freestream_mach_vector(0.6, 2.0, -1.0),
                                  out_format="CSV", out_slip="NO"),
                             4, "explicit"),
+    "output_explicit2d_vtk": (lambda: meshgen.bump_channel_2d(24, 8, 0.08),
+                              dict(solver="EXPLICIT", local="YES", cfl=0.8, mach=(0.6, 0.04, 0),
+                                   out_format="VTK", out_slip="YES"),
+                              6, "explicit"),
+    "output_explicit2d_csv": (lambda: meshgen.bump_channel_2d(24, 8, 0.08),
+                              dict(solver="EXPLICIT", local="NO", cfl=0.8, mach=(0.6, 0.04, 0),
+                                   out_format="CSV", out_slip="NO"),
+                              4, "explicit"),
     "output_implicit_vtk": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
                             dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
                                  mach=(0.84, 0, 0), smoother="DAMPED_JACOBI", lin_tol=1e-2,

@@ -39,7 +39,7 @@ def test_operators_match_oracle(case):
     assert rel_err(got["face_flux"], ref["op_face_flux"]) <= 1e-12
 
 
-@pytest.mark.parametrize("case", EXPLICIT)
+@pytest.mark.parametrize("case", EXPLICIT + G.CASES_2D)
 def test_residual_history_matches_reference(case):
     ref, info = G.load(case)
     mesh = G.mesh_of(info)

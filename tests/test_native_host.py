@@ -53,16 +53,20 @@ def test_build_info_names_sm103a(native):
     assert b"sm_103a" in native.bes_build_info()
 
 
-@pytest.mark.parametrize("case", [c for c in G.CASES])
+@pytest.mark.parametrize("case", G.CASES + G.CASES_2D)
 def test_host_geometry_matches_reference(case):
     ref, info = G.load(case)
     if "geo_volume" not in ref:
         pytest.skip("no geometry dump")
-    g = lib.host_geometry(G.mesh_of(info))
+    mesh = G.mesh_of(info)
+    g = lib.host_geometry(mesh)
     for k in ("volume", "centroid", "face_S", "face_area"):
         np.testing.assert_array_equal(g[k].ravel(), ref["geo_" + k], err_msg=k)
-    for k in ("face_owner", "face_neigh", "face_type", "muscl_slot"):
+    for k in ("face_owner", "face_neigh", "face_type"):
         np.testing.assert_array_equal(g[k].ravel(), ref["geo_" + k], err_msg=k)
+    nfc = mesh.dim + 1  # faces per cell; the fixture pads triangles' fourth slot with -1
+    np.testing.assert_array_equal(g["muscl_slot"][:, :nfc],
+                                  ref["geo_muscl_slot"].reshape(-1, 4)[:, :nfc])
 
 
 def test_renumbering_is_a_permutation_and_groups_faces():
@@ -116,8 +120,11 @@ def test_mesh_errors_are_reported():
         lib.host_geometry(bad2)
 
 
-def test_gmsh_reader_round_trip():
-    m = meshgen.gaussian_box(6, 4, 6)
+@pytest.mark.parametrize("make", [lambda: meshgen.gaussian_box(6, 4, 6),
+                                  lambda: meshgen.bump_channel_2d(12, 4, 0.08)],
+                         ids=["tetrahedra", "triangles"])
+def test_gmsh_reader_round_trip(make):
+    m = make()
     with tempfile.TemporaryDirectory() as d:
         p = os.path.join(d, "m.msh")
         meshgen.write_gmsh(m, p)

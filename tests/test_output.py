@@ -16,7 +16,8 @@ from bes_gb300 import lib
 from tests import _golden as G
 from tests._gpu import context
 
-OUTPUT_CASES = ["output_explicit_vtk", "output_explicit_csv", "output_implicit_vtk"]
+OUTPUT_CASES = ["output_explicit_vtk", "output_explicit_csv", "output_implicit_vtk",
+                "output_explicit2d_vtk", "output_explicit2d_csv"]
 NUM = re.compile(r"^[-+]?(\d+\.?\d*|\.\d+)([eE][-+]?\d+)?$")
 
 
