@@ -59,7 +59,15 @@ WORKLOADS = {
                                              linear_solver_tol=1e-2, linear_solver_max_iter=300,
                                              gmres_restart=30, cfl_ramp_steps=50,
                                              cfl_ramp_start=10.0, cfl_ramp_end=1000.0,
-                                             precision=1)),
+                                             precision=2)),
+    # the same with the FP32 system stored in FP32 (precision 1)
+    "implicit_bump_2m_fp32": dict(kind="implicit", mesh=("bump", 200, 60, 30, 0.08),
+                                  opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
+                                            freestream_mach=(0.84, 0.0, 0.0), linear_solver=1,
+                                            linear_solver_tol=1e-2, linear_solver_max_iter=300,
+                                            gmres_restart=30, cfl_ramp_steps=50,
+                                            cfl_ramp_start=10.0, cfl_ramp_end=1000.0,
+                                            precision=1)),
     # the same scheme on the 120x40x18-hex channel (518,400 tets): a profiling size whose
     # Krylov basis (31 vectors of 10 MB) still exceeds L2
     "implicit_bump_518k": dict(kind="implicit", mesh=("bump", 120, 40, 18, 0.08),
@@ -68,7 +76,7 @@ WORKLOADS = {
                                          linear_solver_tol=1e-2, linear_solver_max_iter=300,
                                          gmres_restart=30, cfl_ramp_steps=50,
                                          cfl_ramp_start=10.0, cfl_ramp_end=1000.0,
-                                         precision=1)),
+                                         precision=2)),
     "implicit_bump_2m_fp64": dict(kind="implicit", mesh=("bump", 200, 60, 30, 0.08),
                                   opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
                                             freestream_mach=(0.84, 0.0, 0.0), linear_solver=1,
@@ -203,14 +211,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profiles(kernel: str, workload: str):
-    """Per-launch DRAM bytes of `kernel` from a committed ncu summary, or None."""
+def traffic_from_profiles(kernel: str, workload: str, precision: int = 1):
+    """Per-launch DRAM bytes of `kernel` (at `precision` for the implicit system) from a
+    committed ncu summary, or None."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         d = json.load(f)
-    return d.get(workload, {}).get(kernel)
+    key = f"{kernel}_packed" if precision == 2 else kernel
+    return d.get(workload, {}).get(key)
 
 
 def cpu_baseline(wl, mesh, steps: int = 2, mach=None):
@@ -292,9 +302,16 @@ def run_reference(args, wl):
 #     four off-diagonal blocks once (4 x 100) + inverse diagonal block (100) + the vector read
 #     and written in both sweeps (4 x 20)                                          = 580
 #   matrix-vector product: five blocks (500) + x (20) + y (20)                       = 540
-# With an FP64 system the block and vector bytes double.
-BYTES_PRECOND = {1: 580.0, 0: 1160.0}
-BYTES_SPMV = {1: 540.0, 0: 1080.0}
+# With an FP64 system the block and vector bytes double.  With 16-bit block-scaled storage
+# (precision 2) a block is 13 half2 words + one FP32 scale = 56 bytes: preconditioner
+# 5 x 56 + 80 = 360, matrix-vector product 5 x 56 + 40 = 320.
+BYTES_PRECOND = {2: 360.0, 1: 580.0, 0: 1160.0}
+BYTES_SPMV = {2: 320.0, 1: 540.0, 0: 1080.0}
+KERNEL_NAMES = {
+    "precond": {2: "block-ILU(0) colour sweeps, packed blocks (ilu_colour_packed_kernel)",
+                1: "block-ILU(0) colour sweeps (ilu_colour_kernel)",
+                0: "block-ILU(0) colour sweeps (ilu_colour_kernel)"},
+    "spmv": {2: "spmv_packed_kernel", 1: "spmv_kernel", 0: "spmv_kernel"}}
 
 
 def implicit_leg(args, torch, ctx, steps, warmup, flush, with_e2e):
@@ -390,7 +407,7 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
     ctx64 = lib.Context(mesh, lib.default_options(**o64))
     plain = implicit_leg(args, torch, ctx64, args.steps, args.warmup, flush, with_e2e=False)
     ctx64.close()
-    prec = 1 if wl["opts"].get("precision") else 0
+    prec = int(wl["opts"].get("precision", 0))
     prof = mixed["prof"]
     cats = {"precond": BYTES_PRECOND[prec] * nc, "spmv": BYTES_SPMV[prec] * nc}
     dom = max(cats, key=lambda k: prof[k][0])
@@ -401,7 +418,10 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
     line = {"metric": METRIC, "metric_full": METRIC_FULL, "value": value, "unit": METRIC,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 system / f64 residual and update",
+            "vs_baseline": None,
+            "dtype": {0: "f64", 1: "f32 system / f64 residual and update",
+                      2: "f32 system stored as fp16 blocks with a power-of-two scale per block "
+                         "/ f64 residual and update"}[prec],
             "data": "synthetic",
             "config": {"workload": args.workload, "cells": nc, "faces": ctx.n_faces,
                        "parallelism": f"replicas{world}",
@@ -421,11 +441,10 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
             "e2e": {"value": world * nc * args.steps / e2e_s, "unit": METRIC,
                     "h2d_bytes_per_step": 40 * nc, "d2h_bytes_per_step": 40 * nc},
             "gpu_launches": mixed["launches"],
-            "roofline": {"kernel": {"precond": "block-ILU(0) colour sweeps (ilu_colour_kernel)",
-                                    "spmv": "spmv_kernel"}[dom],
+            "roofline": {"kernel": KERNEL_NAMES[dom][prec],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": traffic_from_profiles(dom, args.workload),
+                         "traffic": traffic_from_profiles(dom, args.workload, prec),
                          "ms_per_launch": per_launch_ms, "bytes_per_launch": cats[dom],
                          "category_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()}},
             "clocks": clk}
@@ -703,7 +722,7 @@ def main():
             # converged solves/hour to a 1e-8 drop: the FP32-system defect correction against
             # the plain FP64 system, each from the freestream, and their answers compared
             runs = {}
-            for name, prec in (("mixed", 1), ("fp64", 0)):
+            for name, prec in (("mixed", int(wl["opts"].get("precision", 1)) or 1), ("fp64", 0)):
                 o = dict(wl["opts"])
                 o["precision"] = prec
                 c2 = lib.Context(mesh, lib.default_options(**o))

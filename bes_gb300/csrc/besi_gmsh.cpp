@@ -195,8 +195,8 @@ extern "C" int bes_options_from_besi(const char* path, bes_options* o, char* mes
       if (!num(0, x) || x < 1 || x > 200) return bad("GMRES_RESTART must be 1..200");
       o->gmres_restart = (int32_t)x;
     } else if (key == "PRECISION") {  // additive
-      const int w = word({"FP64", "MIXED"});
-      if (w < 0) return bad("PRECISION must be FP64 or MIXED");
+      const int w = word({"FP64", "MIXED", "MIXED_PACKED"});
+      if (w < 0) return bad("PRECISION must be FP64, MIXED or MIXED_PACKED");
       o->precision = w;
     } else if (key == "CFL_RAMP") {  // additive: steps, start, end
       double a, b;

@@ -65,7 +65,7 @@ struct ExplicitGraph {
 namespace bes {
 // Device buffers of the implicit path (allocated when the context is created for it).
 struct ImplicitBuffers {
-  int prec = 0;          // 0: FP64 system, 1: FP32 system (defect correction)
+  int prec = 0;          // 0: FP64 system, 1: FP32 system (defect correction; precision 1 or 2)
   size_t tsize = 8;      // sizeof(T)
   void* A = nullptr;     // ELL blocks [5 slots][25][nc]
   void* LU = nullptr;    // block-ILU(0) factors in the same layout (ILU only)
@@ -76,6 +76,15 @@ struct ImplicitBuffers {
   void* Z = nullptr;     // [5 nc]
   void* W = nullptr;     // [5 nc]
   void* X = nullptr;     // solution dW [5 nc]
+  // precision 2: 16-bit block-scaled copies (half2 [slot][13][nc] + FP32 scale [slot][nc]) of
+  // A (5 slots), the off-diagonal ILU factors (4 slots) and the inverse diagonal (1 slot)
+  bool packed = false;
+  void* A16 = nullptr;
+  float* As = nullptr;
+  void* LU16 = nullptr;
+  float* LUs = nullptr;
+  void* D16 = nullptr;
+  float* Ds = nullptr;
   double* rhs = nullptr;       // FP64 right-hand side [5][nc]
   double* red = nullptr;       // reduction partials [64][kRedBlocks]
   double* red_out = nullptr;   // reduced values [128]

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "context.hpp"
@@ -53,6 +54,9 @@ struct Sys {
   T* Z;
   T* W;
   T* X;
+  bool packed;  // precision 2: the Krylov products and sweeps read the 16-bit copies
+  const __half2 *A16, *LU16, *D16;
+  const float *As, *LUs, *Ds;
   cudaStream_t s;
   explicit Sys(bes_ctx* ctx) : c(ctx) {
     ImplicitBuffers& I = ctx->imp;
@@ -68,6 +72,13 @@ struct Sys {
     Z = (T*)I.Z;
     W = (T*)I.W;
     X = (T*)I.X;
+    packed = I.packed;
+    A16 = (const __half2*)I.A16;
+    LU16 = (const __half2*)I.LU16;
+    D16 = (const __half2*)I.D16;
+    As = I.As;
+    LUs = I.LUs;
+    Ds = I.Ds;
     s = ctx->stream;
   }
   int64_t ldv;  // stride of the Krylov basis: N rounded up to 64 elements (16-byte loads)
@@ -83,6 +94,30 @@ int reduce_to_host(bes_ctx* c, int nrows, int nblocks, int nsum, int sqrt_sums, 
                              c->stream));
   IMP_TRY(c, cudaStreamSynchronize(c->stream));
   return BES_OK;
+}
+
+// 16-bit block-scaled copies (precision 2; T is float there)
+template <class T>
+void enqueue_pack(const Sys<T>& S, const T* src, int slot0, int nslots, void* H, float* sc) {
+  if constexpr (std::is_same<T, float>::value) {
+    pack_blocks_kernel<<<dim3(nblk(S.nc, 256), nslots), 256, 0, S.s>>>(src, slot0, S.nc,
+                                                                       (__half2*)H, sc);
+    ++S.c->launches;
+  }
+}
+
+// y = A x, or y = b - A x when b is given
+template <class T>
+void spmv(const Sys<T>& S, const T* x, const T* b, T* y) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (S.packed) {
+      spmv_packed_kernel<<<nblk(S.nc, 256), 256, 0, S.s>>>(S.c->dm, S.A16, S.As, x, b, y);
+      ++S.c->launches;
+      return;
+    }
+  }
+  spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.c->dm, S.A, x, b, y);
+  ++S.c->launches;
 }
 
 inline bool uses_ilu(const bes_ctx* c) { return c->opt.linear_solver == 1 || c->opt.linear_solver == 2; }
@@ -119,6 +154,10 @@ void enqueue_ilu_factor(const Sys<T>& S) {
       ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
                                                           n, c->imp.ilu_pos, S.LU, S.Dinv);
   }
+  if (S.packed) {
+    enqueue_pack(S, S.LU, 1, 4, c->imp.LU16, c->imp.LUs);
+    enqueue_pack(S, S.Dinv, 0, 1, c->imp.D16, c->imp.Ds);
+  }
 }
 
 // Colour-range sweeps (ilu_colour_kernel) from `in` into S.Z: colours 1..C-2 forward, the last
@@ -131,6 +170,24 @@ void enqueue_ilu_colour_sweeps(const Sys<T>& S, const T* in) {
   const int s1 = M.stage_off[1];
   auto range = [&](int k, int& r0, int& r1) { r0 = M.stage_off[k]; r1 = M.stage_off[k + 1]; };
   int r0, r1;
+  if constexpr (std::is_same<T, float>::value) {
+    if (S.packed) {
+      for (int k = 1; k < C - 1; ++k) {
+        range(k, r0, r1);
+        ilu_colour_packed_kernel<true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
+            c->dm, r0, r1, s1, S.LU16, S.LUs, S.D16, S.Ds, in, S.Z);
+      }
+      range(C - 1, r0, r1);
+      ilu_colour_packed_kernel<true, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
+          c->dm, r0, r1, s1, S.LU16, S.LUs, S.D16, S.Ds, in, S.Z);
+      for (int k = C - 2; k >= 0; --k) {
+        range(k, r0, r1);
+        ilu_colour_packed_kernel<false, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
+            c->dm, r0, r1, s1, S.LU16, S.LUs, S.D16, S.Ds, in, S.Z);
+      }
+      return;
+    }
+  }
   for (int k = 1; k < C - 1; ++k) {
     range(k, r0, r1);
     ilu_colour_kernel<T, true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
@@ -205,6 +262,13 @@ void precond_apply(const Sys<T>& S, const T* in, T* out) {
     cudaGraphLaunch(c->imp.apply_graph, S.s);
     c->launches += 2 * c->soa.n_stages;
   } else {
+    if constexpr (std::is_same<T, float>::value) {
+      if (S.packed) {
+        jacobi_apply_packed_kernel<<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, S.D16, S.Ds, in, out);
+        ++S.c->launches;
+        return;
+      }
+    }
     jacobi_apply_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, S.Dinv, in, out);
     ++S.c->launches;
   }
@@ -255,6 +319,10 @@ int assemble(bes_ctx* c, double cfl, double* norms15) {
                                                uses_ilu(c) ? nullptr : S.Dinv,
                                                c->imp.rhs, S.b, c->imp.red);
   ++S.c->launches;
+  if (S.packed) {
+    enqueue_pack(S, S.A, 0, 5, c->imp.A16, c->imp.As);
+    if (!uses_ilu(c)) enqueue_pack(S, S.Dinv, 0, 1, c->imp.D16, c->imp.Ds);
+  }
   prof_end(c, PROF_ASSEMBLE);
   IMP_TRY(c, cudaGetLastError());
   double r[15];
@@ -310,9 +378,8 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       precond_apply(S, S.Vk(j), S.Z);
       prof_end(c, PROF_PRECOND);
       prof_begin(c, PROF_SPMV);
-      spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.Z, nullptr, S.W);
+      spmv<T>(S, S.Z, nullptr, S.W);
       prof_end(c, PROF_SPMV);
-      ++S.c->launches;
       // classical Gram-Schmidt with a conditional second pass (gs_* kernels); the
       // coefficients stay on the device and reach the host once per iteration
       double* dev = c->imp.red_out;
@@ -365,7 +432,7 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
     precond_apply(S, S.W, S.Z);
     add_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.Z, S.N);
     ++S.c->launches;
-    spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(c->dm, S.A, S.X, S.b, S.W);  // r = b - A x
+    spmv<T>(S, S.X, S.b, S.W);  // r = b - A x
     norm2_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.N, red);
     ++S.c->launches;
     double nr2;
@@ -558,7 +625,13 @@ int implicit_allocate(bes_ctx* c) {
     c->last_error = "GMRES_RESTART must be between 1 and 32";
     return BES_ERR_UNSUPPORTED;
   }
+  if (o.precision < 0 || o.precision > 2) {
+    c->last_error = "precision must be 0 (FP64 system), 1 (FP32 system) or 2 (FP32 system, "
+                    "16-bit block-scaled matrix storage)";
+    return BES_ERR_UNSUPPORTED;
+  }
   I.prec = o.precision ? 1 : 0;
+  I.packed = o.precision == 2;
   I.tsize = I.prec ? sizeof(float) : sizeof(double);
   const SoaMesh& M = c->soa;
   const int64_t nc = M.nc, nf = M.nf, N = 5 * nc;
@@ -572,7 +645,21 @@ int implicit_allocate(bes_ctx* c) {
   }
   if (o.linear_solver == 2) build_ilu_schedule(c->soa, true);
   I.use_colour_ranges = o.linear_solver == 1 && colour_ranges(c->soa);
+  if (I.packed && uses_ilu(c) && !I.use_colour_ranges) {
+    c->last_error = "precision 2 runs block Jacobi or the colour-ordered block ILU(0)";
+    return BES_ERR_UNSUPPORTED;
+  }
   if (uses_ilu(c)) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
+  if (I.packed) {
+    rc |= imp_malloc(c, &I.A16, 5 * 13 * nc * sizeof(__half2));
+    rc |= imp_malloc(c, (void**)&I.As, 5 * nc * sizeof(float));
+    rc |= imp_malloc(c, &I.D16, 13 * nc * sizeof(__half2));
+    rc |= imp_malloc(c, (void**)&I.Ds, nc * sizeof(float));
+    if (uses_ilu(c)) {
+      rc |= imp_malloc(c, &I.LU16, 4 * 13 * nc * sizeof(__half2));
+      rc |= imp_malloc(c, (void**)&I.LUs, 4 * nc * sizeof(float));
+    }
+  }
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
   rc |= imp_malloc(c, &I.b, N * I.tsize);
   rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * basis_stride(nc) * I.tsize);

@@ -11,6 +11,8 @@
 // 20-byte gather (SoA would touch five 32-byte sectors) while streams stay coalesced; the
 // FP64 state and residual keep the solver's [5][nc] layout.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "explicit_kernels.cuh"
 
 namespace bes {
@@ -496,6 +498,152 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, const T* __restric
 #pragma unroll
   for (int r = 0; r < 5; ++r)
     y[(int64_t)i * 5 + r] = b ? b[(int64_t)i * 5 + r] - acc[r] : acc[r];
+}
+
+// ---- 16-bit block-scaled storage of the FP32 system (precision 2)
+// A 5x5 block is stored as 13 half2 words (entries 2p and 2p+1 of the row-major block; the
+// 26th half is 0) in the layout H[slot][13][nc], plus one FP32 scale per block S[slot][nc]:
+// entry q = S * H[q].  The scale is the smallest power of two >= the block's largest |entry|,
+// so the rescaling is exact and every stored entry lies in [-1, 1] with FP16's 11-bit
+// significand; entries below 2^-14 of the scale become FP16 subnormals (absolute error at most
+// 2^-25 of the scale).  Per block: 52 + 4 bytes instead of 100.
+
+// smallest power of two >= x (x >= 0 and finite); 1 for x == 0
+__device__ __forceinline__ float pow2_ceil(float x) {
+  if (x == 0.0f) return 1.0f;
+  const unsigned b = __float_as_uint(x);
+  return __uint_as_float((b + 0x007fffffu) & 0xff800000u);
+}
+
+// pack slots [slot0, slot0 + gridDim.y) of a dense ELL array (or a [25][nc] array with
+// slot0 = 0) into H / S slots [0, gridDim.y); one thread per (cell, slot)
+static __global__ void __launch_bounds__(256) pack_blocks_kernel(const float* __restrict__ A,
+                                                                 int slot0, int nc,
+                                                                 __half2* __restrict__ H,
+                                                                 float* __restrict__ S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (i >= nc) return;
+  float a[26];
+  float mx = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 25; ++q) {
+    a[q] = A[(int64_t)((slot0 + s) * 25 + q) * nc + i];
+    mx = fmaxf(mx, fabsf(a[q]));
+  }
+  a[25] = 0.0f;
+  const float sc = pow2_ceil(mx);
+  const float inv = 1.0f / sc;  // exact: sc is a power of two
+#pragma unroll
+  for (int p = 0; p < 13; ++p)
+    H[(int64_t)(s * 13 + p) * nc + i] = __floats2half2_rn(a[2 * p] * inv, a[2 * p + 1] * inv);
+  S[(int64_t)s * nc + i] = sc;
+}
+
+__device__ __forceinline__ void load_packed(const __half2* __restrict__ H, int s, int nc, int i,
+                                            float* a) {
+#pragma unroll
+  for (int p = 0; p < 13; ++p) {
+    const float2 f = __half22float2(H[(int64_t)(s * 13 + p) * nc + i]);
+    a[2 * p] = f.x;
+    a[2 * p + 1] = f.y;
+  }
+}
+
+// y = A x (or b - A x) with A in packed form: per block, the neighbour's values are scaled
+// by the block's scale and multiplied by the 16-bit entries
+static __global__ void __launch_bounds__(256) spmv_packed_kernel(
+    DevMesh m, const __half2* __restrict__ H, const float* __restrict__ S,
+    const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = m.nc;
+  if (i >= nc) return;
+  float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int j = s == 0 ? i : m.adj[(s - 1) * nc + i];
+    if (j < 0) continue;
+    const float sc = S[(int64_t)s * nc + i];
+    float xs[5], a[26];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) xs[v] = sc * x[(int64_t)j * 5 + v];
+    load_packed(H, s, nc, i, a);
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[r] = fmaf(a[r * 5 + c], xs[c], acc[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+    y[(int64_t)i * 5 + r] = b ? b[(int64_t)i * 5 + r] - acc[r] : acc[r];
+}
+
+// ilu_colour_kernel with packed factors: L / U blocks in H slots 0..3 (local faces 0..3),
+// inv(U_ii) in D (one slot)
+template <bool LOWER, bool UPPER>
+__global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
+    DevMesh m, int r0, int r1, int s1, const __half2* __restrict__ H, const float* __restrict__ HS,
+    const __half2* __restrict__ D, const float* __restrict__ DS, const float* __restrict__ in,
+    float* __restrict__ out) {
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  const int nc = m.nc;
+  const float* own = (LOWER || r0 == 0) ? in : out;
+  float acc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int j = m.adj[s * nc + i];
+    const bool lower = LOWER && j >= 0 && j < r0;
+    const bool upper = UPPER && j >= r1;
+    if (!lower && !upper) continue;
+    const float* src = (lower && j < s1) ? in : out;
+    const float sc = HS[(int64_t)s * nc + i];
+    float y[5], a[26];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) y[v] = sc * src[(int64_t)j * 5 + v];
+    load_packed(H, s, nc, i, a);
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[r] = fmaf(-a[r * 5 + c], y[c], acc[r]);
+  }
+  if (UPPER) {
+    float a[26];
+    load_packed(D, 0, nc, i, a);
+    const float sc = DS[i];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      float x = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) x = fmaf(a[r * 5 + c], acc[c], x);
+      out[(int64_t)i * 5 + r] = sc * x;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[(int64_t)i * 5 + v] = acc[v];
+  }
+}
+
+// block-Jacobi application with a packed inverse diagonal
+static __global__ void __launch_bounds__(256) jacobi_apply_packed_kernel(
+    int nc, const __half2* __restrict__ D, const float* __restrict__ DS,
+    const float* __restrict__ in, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  float x[5], a[26];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) x[v] = in[(int64_t)i * 5 + v];
+  load_packed(D, 0, nc, i, a);
+  const float sc = DS[i];
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) acc = fmaf(a[r * 5 + c], x[c], acc);
+    out[(int64_t)i * 5 + r] = sc * acc;
+  }
 }
 
 // Per-thread accumulation type of the vector kernels: the FP32 system accumulates each

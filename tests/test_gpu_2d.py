@@ -36,13 +36,16 @@ def test_2d_implicit_reaches_the_explicit_steady_state():
     mesh = meshgen.bump_channel_2d(24, 8, 0.02)
     mach = (0.4, 0.0, 0.0)
     imp = _implicit(mesh, freestream_mach=mach)
-    h_imp = np.concatenate([imp.implicit_steps(40) for _ in range(2)])
+    # L2 of the unscaled residual R (implicit columns 14-18, explicit 0-4); the implicit
+    # solve falls by about 0.86 per step once the CFL ramp is done
+    h_imp = imp.implicit_steps(50)
+    while h_imp[-1, 14:19].max() > 1e-11 * h_imp[0, 14:19].max() and len(h_imp) < 400:
+        h_imp = np.concatenate([h_imp, imp.implicit_steps(50)])
     exp = context(mesh, solver_type=0, local_time_step=1, courant_num=0.8, freestream_mach=mach)
     h_exp = np.concatenate([exp.explicit_iterations(2000) for _ in range(4)])
-    # L2 of the unscaled residual R (implicit columns 14-18, explicit 0-4)
     drop_imp = h_imp[-1, 14:19].max() / h_imp[0, 14:19].max()
     drop_exp = h_exp[-1, :5].max() / h_exp[0, :5].max()
-    assert drop_imp <= 1e-11 and drop_exp <= 1e-11, (drop_imp, drop_exp)
+    assert drop_imp <= 1e-11 and drop_exp <= 1e-11, (len(h_imp), drop_imp, drop_exp)
     u_imp, u_exp = imp.get_state(), exp.get_state()
     assert rel_err(u_imp, u_exp) <= 1e-7
     # no spanwise momentum on a 2-D mesh, and no residual for it

@@ -115,6 +115,43 @@ def test_fp32_defect_correction_tracks_fp64(precond):
     assert np.all(h32[:, 12] >= 1)
 
 
+@pytest.mark.parametrize("precond", [0, 1])
+def test_packed_storage_tracks_fp64(precond):
+    """precision 2 (FP16 blocks with a power-of-two scale per block) perturbs the linear
+    systems by about 2^-11 relative; the steps follow the FP64 system as closely as FP32."""
+    mesh = meshgen.bump_channel(24, 8, 6, 0.08)
+    kw = dict(solver_type=1, local_time_step=1, courant_num=10.0, freestream_mach=(0.84, 0, 0),
+              linear_solver=precond, linear_solver_tol=1e-2, linear_solver_max_iter=300,
+              cfl_ramp_steps=10, cfl_ramp_start=10.0, cfl_ramp_end=200.0)
+    c64 = context(mesh, **kw)
+    c16 = context(mesh, precision=2, **kw)
+    h64 = c64.implicit_steps(20)
+    h16 = c16.implicit_steps(20)
+    assert rel_err(c16.get_state(), c64.get_state()) <= 1e-3
+    assert np.max(np.abs(np.log(h16[:, :5] / h64[:, :5]))) <= 0.05
+    # linear iterations per step within 20 % of the FP64 system's
+    assert abs(h16[:, 12].sum() - h64[:, 12].sum()) <= 0.2 * h64[:, 12].sum()
+
+
+def test_packed_storage_converges_to_the_fp64_steady_state():
+    """Defect correction: the residual and the update are FP64, so the 16-bit matrix changes
+    the path, not the fixed point.  A 4 % bump at Mach 0.5, where the oracle's FP64 implicit
+    solve falls by 5e-14 in 150 steps (an 8 % bump stalls near 3e-5)."""
+    mesh = meshgen.bump_channel(24, 8, 6, 0.04)
+    kw = dict(solver_type=1, local_time_step=1, courant_num=10.0, freestream_mach=(0.5, 0, 0),
+              linear_solver=1, linear_solver_tol=1e-2, linear_solver_max_iter=300,
+              cfl_ramp_steps=10, cfl_ramp_start=10.0, cfl_ramp_end=1000.0)
+    states = []
+    for prec in (0, 2):
+        ctx = context(mesh, precision=prec, **kw)
+        h = ctx.implicit_steps(40)
+        while h[-1, 14:19].max() > 1e-11 * h[0, 14:19].max() and len(h) < 400:
+            h = np.concatenate([h, ctx.implicit_steps(40)])
+        assert h[-1, 14:19].max() <= 1e-11 * h[0, 14:19].max(), (prec, len(h))
+        states.append(ctx.get_state())
+    assert rel_err(states[1], states[0]) <= 1e-9
+
+
 @pytest.mark.parametrize("linear_solver", [1, 2])
 def test_ilu_orders_match_oracle(linear_solver):
     """Colour-ordered (1) and RCM-ordered level-scheduled (2) block ILU(0): the GPU's

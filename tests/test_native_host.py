@@ -173,6 +173,14 @@ SAVE_INTERVAL = 10
     assert o.linear_solver_tol == 1e-2 and o.number_of_time_step == 7
     # untouched defaults (src/Config.cpp:73-114)
     assert o.venkatakrishnan_factor == 5.0 and o.harten_correction_limit == 0.05
+    assert o.precision == 0
+
+
+@pytest.mark.parametrize("word,value", [("FP64", 0), ("MIXED", 1), ("MIXED_PACKED", 2)])
+def test_besi_precision_key(word, value):
+    with tempfile.TemporaryDirectory() as d:
+        o, _ = lib.options_from_besi(_write(d, f"PRECISION = {word}\n"))
+    assert o.precision == value
     assert o.gas_constant == 287.0 and o.specific_heat_ratio == 1.4
 
 
