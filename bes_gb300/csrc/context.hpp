@@ -85,6 +85,10 @@ struct ImplicitBuffers {
   float* LUs = nullptr;
   void* D16 = nullptr;
   float* Ds = nullptr;
+  // precision 2: Krylov basis V in FP16 (kBasisScale times the value) and an FP32 copy of its
+  // newest vector, the preconditioner's input
+  bool basis16 = false;
+  void* Vx = nullptr;
   double* rhs = nullptr;       // FP64 right-hand side [5][nc]
   double* red = nullptr;       // reduction partials [64][kRedBlocks]
   double* red_out = nullptr;   // reduced values [128]

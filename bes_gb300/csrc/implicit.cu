@@ -57,6 +57,8 @@ struct Sys {
   bool packed;  // precision 2: the Krylov products and sweeps read the 16-bit copies
   const __half2 *A16, *LU16, *D16;
   const float *As, *LUs, *Ds;
+  bool basis16;  // precision 2: FP16 Krylov basis; the preconditioner reads Vx
+  T* Vx;         // FP32 copy of the newest basis vector (basis16 only)
   cudaStream_t s;
   explicit Sys(bes_ctx* ctx) : c(ctx) {
     ImplicitBuffers& I = ctx->imp;
@@ -79,6 +81,8 @@ struct Sys {
     As = I.As;
     LUs = I.LUs;
     Ds = I.Ds;
+    basis16 = I.basis16;
+    Vx = (T*)I.Vx;
     s = ctx->stream;
   }
   int64_t ldv;  // stride of the Krylov basis: N rounded up to 64 elements (16-byte loads)
@@ -226,9 +230,10 @@ int ensure_ilu_graphs(const Sys<T>& S) {
   IMP_TRY(c, cudaGraphInstantiate(&c->imp.factor_graph, g, 0));
   cudaGraphDestroy(g);
   if (c->imp.use_colour_ranges) {
-    const int nin = c->opt.gmres_restart + 2;  // V_0..V_m, then W
+    // inputs V_0..V_m, then W; with an FP16 basis the FP32 copy Vx, then W
+    const int nin = S.basis16 ? 2 : c->opt.gmres_restart + 2;
     for (int q = 0; q < nin; ++q) {
-      const T* in = q + 1 < nin ? S.Vk(q) : S.W;
+      const T* in = q + 1 < nin ? (S.basis16 ? S.Vx : S.Vk(q)) : S.W;
       IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
       enqueue_ilu_colour_sweeps(S, in);
       IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
@@ -252,8 +257,10 @@ template <class T>
 void precond_apply(const Sys<T>& S, const T* in, T* out) {
   bes_ctx* c = S.c;
   if (uses_ilu(c) && c->imp.use_colour_ranges) {
-    // out is S.Z; in is one of V_0..V_m (graph q = its index) or W (the last graph)
-    const int64_t q = in == S.W ? (int64_t)c->imp.colour_graphs.size() - 1 : (in - S.V) / S.ldv;
+    // out is S.Z; in is one of V_0..V_m (graph q = its index) or Vx (graph 0), or W (the
+    // last graph)
+    const int64_t q = in == S.W ? (int64_t)c->imp.colour_graphs.size() - 1
+                                : (S.basis16 ? 0 : (in - S.V) / S.ldv);
     cudaGraphLaunch(c->imp.colour_graphs[q], S.s);
     c->launches += 2 * c->soa.n_stages - 1;
   } else if (uses_ilu(c)) {
@@ -339,9 +346,17 @@ int assemble(bes_ctx* c, double cfl, double* norms15) {
 
 // Right-preconditioned GMRES(m), x0 = 0, classical Gram-Schmidt with a conditional second
 // pass, Givens rotations; stops when |g_{j+1}| <= tol |b| (AMGCL gmres.hpp:163,214 semantics).
-template <class T>
-int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
+template <class T, class B>
+int gmres_basis(bes_ctx* c, int& iters_out, double& rel_out) {
   Sys<T> S(c);
+  constexpr bool kBasis16 = !std::is_same<T, B>::value;
+  B* const Vb = (B*)c->imp.V;
+  auto Vk = [&](int k) { return Vb + (int64_t)k * S.ldv; };
+  // the preconditioner's input: the basis vector itself, or its FP32 copy
+  auto pin = [&](int k) -> const T* {
+    if constexpr (kBasis16) return S.Vx;
+    else return Vk(k);
+  };
   const bes_options& o = c->opt;
   const int mr = o.gmres_restart;
   const int maxiter = o.linear_solver_max_iter;
@@ -368,14 +383,17 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
   ++S.c->launches;
   while (true) {
     if (beta < eps || iter >= maxiter) break;
-    scale_kernel<T><<<G, 256, 0, S.s>>>(S.Vk(0), S.W, 1.0 / beta, S.N);
+    if constexpr (kBasis16)
+      basis_start_kernel<<<G, 256, 0, S.s>>>(Vk(0), S.Vx, S.W, 1.0 / beta, S.N);
+    else
+      scale_kernel<T><<<G, 256, 0, S.s>>>(Vk(0), S.W, 1.0 / beta, S.N);
     ++S.c->launches;
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
     while (j < mr && iter < maxiter) {
       prof_begin(c, PROF_PRECOND);
-      precond_apply(S, S.Vk(j), S.Z);
+      precond_apply(S, pin(j), S.Z);
       prof_end(c, PROF_PRECOND);
       prof_begin(c, PROF_SPMV);
       spmv<T>(S, S.Z, nullptr, S.W);
@@ -385,15 +403,19 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       double* dev = c->imp.red_out;
       const int nv = j + 1;
       prof_begin(c, PROF_ORTHO);
-      launch_gs_dots<T>(nv, G, S.s, S.V, S.ldv, S.W, S.N, red);
+      T* const vx = kBasis16 ? S.Vx : nullptr;
+      launch_gs_dots<T, B>(nv, G, S.s, Vb, S.ldv, S.W, S.N, red);
       reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev);
       float* devf = c->imp.red_out_f;
       gs_decide_kernel<<<1, 64, 0, S.s>>>(dev, devf, nv, 1);
-      launch_gs_update<T, GS_FINAL1>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, devf, S.N, red);
-      launch_gs_update<T, GS_REORTH>(nv, G, S.s, nullptr, S.W, S.V, S.ldv, dev, devf, S.N, red);
+      launch_gs_update<T, B, GS_FINAL1>(nv, G, S.s, Vk(j + 1), vx, S.W, Vb, S.ldv, dev, devf,
+                                        S.N, red);
+      launch_gs_update<T, B, GS_REORTH>(nv, G, S.s, nullptr, nullptr, S.W, Vb, S.ldv, dev, devf,
+                                        S.N, red);
       reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev + kGsH2);
       gs_decide_kernel<<<1, 64, 0, S.s>>>(dev, devf, nv, 2);
-      launch_gs_update<T, GS_FINAL2>(nv, G, S.s, S.Vk(j + 1), S.W, S.V, S.ldv, dev, devf, S.N, red);
+      launch_gs_update<T, B, GS_FINAL2>(nv, G, S.s, Vk(j + 1), vx, S.W, Vb, S.ldv, dev, devf,
+                                        S.N, red);
       prof_end(c, PROF_ORTHO);
       S.c->launches += 8;
       double hbuf[kGsScalars];
@@ -427,7 +449,7 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
       y[i] = s / H[i * mr + i];
     }
     IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, S.s));
-    lincomb_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.V, S.ldv, j, c->imp.coef, S.N);
+    lincomb_kernel<T, B><<<G, 256, 0, S.s>>>(S.W, Vb, S.ldv, j, c->imp.coef, S.N);
     ++S.c->launches;
     precond_apply(S, S.W, S.Z);
     add_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.Z, S.N);
@@ -445,6 +467,13 @@ int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
   rel_out = norm_r / norm_b;
   IMP_TRY(c, cudaGetLastError());
   return BES_OK;
+}
+
+template <class T>
+int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
+  if constexpr (std::is_same<T, float>::value)
+    if (c->imp.basis16) return gmres_basis<float, __half>(c, iters_out, rel_out);
+  return gmres_basis<T, T>(c, iters_out, rel_out);
 }
 
 double cfl_for_step(const bes_ctx* c) {
@@ -662,7 +691,10 @@ int implicit_allocate(bes_ctx* c) {
   }
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
   rc |= imp_malloc(c, &I.b, N * I.tsize);
-  rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * basis_stride(nc) * I.tsize);
+  I.basis16 = I.packed;
+  rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * basis_stride(nc) *
+                                (I.basis16 ? sizeof(__half) : I.tsize));
+  if (I.basis16) rc |= imp_malloc(c, &I.Vx, N * sizeof(float));
   rc |= imp_malloc(c, &I.Z, N * I.tsize);
   rc |= imp_malloc(c, &I.W, N * I.tsize);
   rc |= imp_malloc(c, &I.X, N * I.tsize);

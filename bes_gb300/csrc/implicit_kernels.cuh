@@ -13,6 +13,8 @@
 #pragma once
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "explicit_kernels.cuh"
 
 namespace bes {
@@ -30,7 +32,7 @@ __device__ __forceinline__ T ellc(const T* A, int s, int q, int nc, int i) {
 
 // 5x5 inverse by Gauss-Jordan elimination with partial pivoting.
 template <class T>
-__device__ void inv5(const T* a, T* inv) {
+__device__ __forceinline__ void inv5(const T* a, T* inv) {
   T m[5][10];
 #pragma unroll
   for (int i = 0; i < 5; ++i)
@@ -41,17 +43,25 @@ __device__ void inv5(const T* a, T* inv) {
     }
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
+    // pivot: the first row r >= c with the largest |m[r][c]|; the swap is written with
+    // compile-time row indices (predicated), so m stays in registers
     int p = c;
+    T best = fabs(m[c][c]);
 #pragma unroll
     for (int r = c + 1; r < 5; ++r)
-      if (fabs(m[r][c]) > fabs(m[p][c])) p = r;
-    if (p != c)
-#pragma unroll
-      for (int j = 0; j < 10; ++j) {
-        const T t = m[p][j];
-        m[p][j] = m[c][j];
-        m[c][j] = t;
+      if (fabs(m[r][c]) > best) {
+        best = fabs(m[r][c]);
+        p = r;
       }
+#pragma unroll
+    for (int r = c + 1; r < 5; ++r)
+      if (r == p)
+#pragma unroll
+        for (int j = 0; j < 10; ++j) {
+          const T t = m[r][j];
+          m[r][j] = m[c][j];
+          m[c][j] = t;
+        }
     const T piv = T(1) / m[c][c];
 #pragma unroll
     for (int j = 0; j < 10; ++j) m[c][j] *= piv;
@@ -277,20 +287,31 @@ __global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_
     nbr[s] = m.adj[s * nc + i];
     pn[s] = nbr[s] >= 0 ? (RANGE ? nbr[s] : pos[nbr[s]]) : 0x7fffffff;
   }
-  // lower slots sorted by position
-  int lo[4], nl = 0;
-  for (int s = 0; s < 4; ++s)
-    if (nbr[s] >= 0 && pn[s] < pi) lo[nl++] = s;
-  for (int a = 1; a < nl; ++a)
-    for (int b = a; b > 0 && pn[lo[b]] < pn[lo[b - 1]]; --b) {
-      const int x = lo[b];
-      lo[b] = lo[b - 1];
-      lo[b - 1] = x;
-    }
+  // lower slots in increasing position: rank[s] = number of lower slots before slot s (the
+  // neighbours are distinct cells, so positions are distinct).  All indexing of nbr / pn / rank
+  // uses compile-time indices, so they stay in registers.
+  bool low[4];
+  int rank[4], nl = 0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    low[s] = nbr[s] >= 0 && pn[s] < pi;
+    nl += low[s];
+  }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    rank[s] = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) rank[s] += (low[t] && pn[t] < pn[s]) ? 1 : 0;
+  }
   for (int li = 0; li < nl; ++li) {
-    const int s = lo[li];
-    const int j = nbr[s];
-    const int pj = pn[s];
+    int s = 0, j = 0, pj = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (low[t] && rank[t] == li) {
+        s = t;
+        j = nbr[t];
+        pj = pn[t];
+      }
     T L[25];
 #pragma unroll
     for (int r = 0; r < 5; ++r)
@@ -304,6 +325,7 @@ __global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_
 #pragma unroll
     for (int q = 0; q < 25; ++q) ell(A, 1 + s, q, nc, i) = L[q];
     // A_ik -= L_ij U_jk for every k in row i's pattern with pos(k) > pos(j) and (j,k) present
+#pragma unroll 1
     for (int kk = -1; kk < 4; ++kk) {
       const int col = kk < 0 ? i : nbr[kk];
       if (kk >= 0 && (col < 0 || pn[kk] <= pj)) continue;
@@ -720,28 +742,101 @@ struct alignas(16) Pack16 {
   T v[W];
 };
 
+// Element type B of the Krylov basis: the vector type T itself, or (precision 2) FP16 holding
+// kBasisScale times the value.  A basis vector has unit norm, so |entries| <= 1 and the scaled
+// entries stay below 2^14 (FP16 overflows at 65504); entries under 2^-28 lose relative
+// precision as FP16 subnormals (absolute error at most 2^-39).
+constexpr float kBasisScale = 16384.0f;
+constexpr float kBasisInvScale = 1.0f / 16384.0f;
+
+// W consecutive basis entries (16 bytes of basis per access: 16 / sizeof(T) entries of T, or
+// eight FP16 entries; W is a multiple of the vector granule Pack16<T>::W)
+template <class T, class B>
+struct BasisIO {
+  static constexpr int W = 16 / sizeof(T);
+  template <class A>
+  __device__ static __forceinline__ void load(const B* V, int64_t g, A* x) {
+    const Pack16<T> p = reinterpret_cast<const Pack16<T>*>(V)[g];
+#pragma unroll
+    for (int e = 0; e < W; ++e) x[e] = (A)p.v[e];
+  }
+  template <class A>
+  __device__ static __forceinline__ void store(B* V, int64_t g, const A* x) {
+    Pack16<T> p;
+#pragma unroll
+    for (int e = 0; e < W; ++e) p.v[e] = (T)x[e];
+    reinterpret_cast<Pack16<T>*>(V)[g] = p;
+  }
+  template <class A>
+  __device__ static __forceinline__ A get(const B* V, int64_t i) { return (A)V[i]; }
+  template <class A>
+  __device__ static __forceinline__ void set(B* V, int64_t i, A x) { V[i] = (T)x; }
+};
+template <>
+struct BasisIO<float, __half> {
+  static constexpr int W = 8;  // 16-byte loads of eight FP16 entries
+  template <class A>
+  __device__ static __forceinline__ void load(const __half* V, int64_t g, A* x) {
+    const uint4 u = reinterpret_cast<const uint4*>(V)[g];
+    const unsigned w4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w4[q]));
+      x[2 * q] = f.x * kBasisInvScale;
+      x[2 * q + 1] = f.y * kBasisInvScale;
+    }
+  }
+  template <class A>
+  __device__ static __forceinline__ void store(__half* V, int64_t g, const A* x) {
+    unsigned w4[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const __half2 h = __floats2half2_rn(x[2 * q] * kBasisScale, x[2 * q + 1] * kBasisScale);
+      w4[q] = *reinterpret_cast<const unsigned*>(&h);
+    }
+    reinterpret_cast<uint4*>(V)[g] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+  }
+  template <class A>
+  __device__ static __forceinline__ A get(const __half* V, int64_t i) {
+    return __half2float(V[i]) * kBasisInvScale;
+  }
+  template <class A>
+  __device__ static __forceinline__ void set(__half* V, int64_t i, A x) {
+    V[i] = __float2half_rn(x * kBasisScale);
+  }
+};
+
 // Pass 1: partial V_k . w (rows k < NV) and |w|^2 (row NV).
-template <class T, int NV>
-__global__ void __launch_bounds__(256) gs_dots_kernel(const T* __restrict__ V, int64_t ldv,
+template <class T, class B, int NV>
+__global__ void __launch_bounds__(256) gs_dots_kernel(const B* __restrict__ V, int64_t ldv,
                                                       const T* __restrict__ w, int64_t N,
                                                       double* __restrict__ partials) {
   typedef typename AccType<T>::type A;
   typedef Pack16<T> P;
-  constexpr int W = P::W;
+  typedef BasisIO<T, B> IO;
+  constexpr int W = IO::W;      // entries per granule
+  constexpr int NP = W / P::W;  // 16-byte vector packs per granule
   A acc[NV + 1];
 #pragma unroll
   for (int k = 0; k <= NV; ++k) acc[k] = A(0);
   const int64_t ng = N / W;
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng;
        g += (int64_t)gridDim.x * blockDim.x) {
-    const P wv = reinterpret_cast<const P*>(w)[g];
+    A wv[W];
 #pragma unroll
-    for (int e = 0; e < W; ++e) acc[NV] += (A)wv.v[e] * (A)wv.v[e];
+    for (int p = 0; p < NP; ++p) {
+      const P q = reinterpret_cast<const P*>(w)[g * NP + p];
+#pragma unroll
+      for (int e = 0; e < P::W; ++e) wv[p * P::W + e] = (A)q.v[e];
+    }
+#pragma unroll
+    for (int e = 0; e < W; ++e) acc[NV] += wv[e] * wv[e];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const P vk = reinterpret_cast<const P*>(V + (int64_t)k * ldv)[g];
+      A vk[W];
+      IO::load(V + (int64_t)k * ldv, g, vk);
 #pragma unroll
-      for (int e = 0; e < W; ++e) acc[k] += (A)vk.v[e] * (A)wv.v[e];
+      for (int e = 0; e < W; ++e) acc[k] += vk[e] * wv[e];
     }
   }
   if (blockIdx.x == 0 && threadIdx.x < N - ng * W) {  // the ragged tail, < W elements
@@ -749,7 +844,7 @@ __global__ void __launch_bounds__(256) gs_dots_kernel(const T* __restrict__ V, i
     const A x = (A)w[i];
     acc[NV] += x * x;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] += (A)V[(int64_t)k * ldv + i] * x;
+    for (int k = 0; k < NV; ++k) acc[k] += IO::template get<A>(V + (int64_t)k * ldv, i) * x;
   }
   block_reduce_store<NV + 1, A>(acc, partials);
 }
@@ -792,17 +887,21 @@ static __global__ void gs_decide_kernel(double* __restrict__ dev, float* __restr
 enum GsMode { GS_FINAL1 = 0, GS_REORTH = 1, GS_FINAL2 = 2 };
 
 // FINAL1 / FINAL2: out = (w - sum_k c_k V_k) * dev[kGsInv] with c = h (FINAL1, runs without
-// a second pass) or h2 (FINAL2, runs with one).  REORTH: w -= sum_k h_k V_k in place, with
-// partial V_k . w (rows k < NV) and |w|^2 (row NV) of the result.
-template <class T, int NV, int MODE>
-__global__ void __launch_bounds__(256) gs_update_kernel(T* __restrict__ out, T* w,
-                                                        const T* __restrict__ V, int64_t ldv,
+// a second pass) or h2 (FINAL2, runs with one); with an FP16 basis the new vector also goes to
+// outx in T (the preconditioner's input).  REORTH: w -= sum_k h_k V_k in place, with partial
+// V_k . w (rows k < NV) and |w|^2 (row NV) of the result.
+template <class T, class B, int NV, int MODE>
+__global__ void __launch_bounds__(256) gs_update_kernel(B* __restrict__ out, T* __restrict__ outx,
+                                                        T* w, const B* __restrict__ V, int64_t ldv,
                                                         const double* __restrict__ dev,
                                                         const float* __restrict__ devf,
                                                         int64_t N, double* __restrict__ partials) {
   typedef typename AccType<T>::type A;
   typedef Pack16<T> P;
-  constexpr int W = P::W;
+  typedef BasisIO<T, B> IO;
+  constexpr int W = IO::W;      // entries per granule
+  constexpr int NP = W / P::W;  // 16-byte vector packs per granule
+  constexpr bool kCopy = !std::is_same<T, B>::value;
   const A* cf = gs_coef<A>(dev, devf);
   const bool second = cf[kGsFlag] != A(0);
   const bool runs = MODE == GS_FINAL1 ? !second : second;
@@ -820,51 +919,74 @@ __global__ void __launch_bounds__(256) gs_update_kernel(T* __restrict__ out, T* 
   const int64_t ng = N / W;
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng;
        g += (int64_t)gridDim.x * blockDim.x) {
-    const P wv = reinterpret_cast<const P*>(w)[g];
     A x[W];
 #pragma unroll
-    for (int e = 0; e < W; ++e) x[e] = (A)wv.v[e];
+    for (int p = 0; p < NP; ++p) {
+      const P q = reinterpret_cast<const P*>(w)[g * NP + p];
+#pragma unroll
+      for (int e = 0; e < P::W; ++e) x[p * P::W + e] = (A)q.v[e];
+    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const P vk = reinterpret_cast<const P*>(V + (int64_t)k * ldv)[g];
+      A vk[W];
+      IO::load(V + (int64_t)k * ldv, g, vk);
 #pragma unroll
-      for (int e = 0; e < W; ++e) x[e] -= c[k] * (A)vk.v[e];
+      for (int e = 0; e < W; ++e) x[e] -= c[k] * vk[e];
     }
-    P o;
     if (MODE == GS_REORTH) {
+      A xr[W];
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        o.v[e] = (T)x[e];
-        acc[NV] += (A)o.v[e] * (A)o.v[e];
+      for (int p = 0; p < NP; ++p) {
+        P o;
+#pragma unroll
+        for (int e = 0; e < P::W; ++e) {
+          o.v[e] = (T)x[p * P::W + e];
+          xr[p * P::W + e] = (A)o.v[e];
+        }
+        reinterpret_cast<P*>(w)[g * NP + p] = o;
       }
+#pragma unroll
+      for (int e = 0; e < W; ++e) acc[NV] += xr[e] * xr[e];
       // the second pass is rare: V is read again (from L2) for its dot products rather than
       // held in registers
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
-        const P vk = reinterpret_cast<const P*>(V + (int64_t)k * ldv)[g];
+        A vk[W];
+        IO::load(V + (int64_t)k * ldv, g, vk);
 #pragma unroll
-        for (int e = 0; e < W; ++e) acc[k] += (A)vk.v[e] * (A)o.v[e];
+        for (int e = 0; e < W; ++e) acc[k] += vk[e] * xr[e];
       }
-      reinterpret_cast<P*>(w)[g] = o;
     } else {
+      A y[W];
 #pragma unroll
-      for (int e = 0; e < W; ++e) o.v[e] = (T)(x[e] * inv);
-      reinterpret_cast<P*>(out)[g] = o;
+      for (int e = 0; e < W; ++e) y[e] = (A)(T)(x[e] * inv);
+      IO::store(out, g, y);
+      if (kCopy) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          P o;
+#pragma unroll
+          for (int e = 0; e < P::W; ++e) o.v[e] = (T)y[p * P::W + e];
+          reinterpret_cast<P*>(outx)[g * NP + p] = o;
+        }
+      }
     }
   }
   if (blockIdx.x == 0 && threadIdx.x < N - ng * W) {  // the ragged tail
     const int64_t i = ng * W + threadIdx.x;
     A x = (A)w[i];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) x -= c[k] * (A)V[(int64_t)k * ldv + i];
+    for (int k = 0; k < NV; ++k) x -= c[k] * IO::template get<A>(V + (int64_t)k * ldv, i);
     if (MODE == GS_REORTH) {
       const T xt = (T)x;
       w[i] = xt;
       acc[NV] += (A)xt * (A)xt;
 #pragma unroll
-      for (int k = 0; k < NV; ++k) acc[k] += (A)V[(int64_t)k * ldv + i] * (A)xt;
+      for (int k = 0; k < NV; ++k) acc[k] += IO::template get<A>(V + (int64_t)k * ldv, i) * (A)xt;
     } else {
-      out[i] = (T)(x * inv);
+      const T y = (T)(x * inv);
+      IO::template set<A>(out, i, (A)y);
+      if (kCopy) outx[i] = y;
     }
   }
   if (MODE == GS_REORTH) block_reduce_store<NA, A>(acc, partials);
@@ -875,24 +997,25 @@ __global__ void __launch_bounds__(256) gs_update_kernel(T* __restrict__ out, T* 
   X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) \
   X(17) X(18) X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27) X(28) X(29) X(30) X(31) X(32)
 
-template <class T>
-void launch_gs_dots(int nvec, int G, cudaStream_t s, const T* V, int64_t ldv, const T* w,
+template <class T, class B>
+void launch_gs_dots(int nvec, int G, cudaStream_t s, const B* V, int64_t ldv, const T* w,
                     int64_t N, double* partials) {
   switch (nvec) {
 #define BES_DOTS_CASE(n) \
-  case n: gs_dots_kernel<T, n><<<G, 256, 0, s>>>(V, ldv, w, N, partials); break;
+  case n: gs_dots_kernel<T, B, n><<<G, 256, 0, s>>>(V, ldv, w, N, partials); break;
     BES_NV_CASES(BES_DOTS_CASE)
 #undef BES_DOTS_CASE
     default: break;
   }
 }
 
-template <class T, int MODE>
-void launch_gs_update(int nvec, int G, cudaStream_t s, T* out, T* w, const T* V, int64_t ldv,
-                      const double* dev, const float* devf, int64_t N, double* partials) {
+template <class T, class B, int MODE>
+void launch_gs_update(int nvec, int G, cudaStream_t s, B* out, T* outx, T* w, const B* V,
+                      int64_t ldv, const double* dev, const float* devf, int64_t N,
+                      double* partials) {
   switch (nvec) {
 #define BES_UPD_CASE(n) \
-  case n: gs_update_kernel<T, n, MODE><<<G, 256, 0, s>>>(out, w, V, ldv, dev, devf, N, partials); break;
+  case n: gs_update_kernel<T, B, n, MODE><<<G, 256, 0, s>>>(out, outx, w, V, ldv, dev, devf, N, partials); break;
     BES_NV_CASES(BES_UPD_CASE)
 #undef BES_UPD_CASE
     default: break;
@@ -910,8 +1033,8 @@ __global__ void __launch_bounds__(256) scale_kernel(T* __restrict__ out, const T
 }
 
 // out = sum_k y_k V_k
-template <class T>
-__global__ void __launch_bounds__(256) lincomb_kernel(T* __restrict__ out, const T* __restrict__ V,
+template <class T, class B>
+__global__ void __launch_bounds__(256) lincomb_kernel(T* __restrict__ out, const B* __restrict__ V,
                                                       int64_t ldv, int nvec,
                                                       const double* __restrict__ y, int64_t N) {
   typedef typename AccType<T>::type A;
@@ -921,8 +1044,23 @@ __global__ void __launch_bounds__(256) lincomb_kernel(T* __restrict__ out, const
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
        idx += (int64_t)gridDim.x * blockDim.x) {
     A x = A(0);
-    for (int k = 0; k < nvec; ++k) x += ys[k] * (A)V[(int64_t)k * ldv + idx];
+    for (int k = 0; k < nvec; ++k) x += ys[k] * BasisIO<T, B>::template get<A>(V + (int64_t)k * ldv, idx);
     out[idx] = (T)x;
+  }
+}
+
+// First basis vector from an FP32 residual: V_0 = s r in the basis's format, and its FP32
+// copy x0 (the preconditioner's input)
+static __global__ void __launch_bounds__(256) basis_start_kernel(__half* __restrict__ V0,
+                                                                 float* __restrict__ x0,
+                                                                 const float* __restrict__ r,
+                                                                 double s, int64_t N) {
+  const float sf = (float)s;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const float y = r[idx] * sf;
+    x0[idx] = y;
+    BasisIO<float, __half>::set<float>(V0, idx, y);
   }
 }
 

@@ -80,7 +80,8 @@ typedef struct {
   int32_t jacobian_repeat;        /* times each Jacobian block is added (Q9, default 5) */
   int32_t precision;              /* PRECISION (additive): 0 FP64, 1 FP32 linear solve,
                                      2 FP32 linear solve with the matrix and factors stored
-                                     as FP16 blocks with a power-of-two scale per block */
+                                     as FP16 blocks with a power-of-two scale per block and
+                                     the Krylov basis stored in FP16 */
   int32_t cfl_ramp_steps;         /* CFL_RAMP (additive): steps of a geometric CFL ramp, 0 off */
   int32_t freestream_ramp;        /* FREESTREAM_RAMP: steps over which the freestream velocity
                                      ramps up (src/Config.cpp:688-706), 0 off */
@@ -140,7 +141,8 @@ int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
  * colour-ordered block-ILU(0) (1) or RCM-ordered level-scheduled block-ILU(0) (2)
  * preconditioner, in FP64 (precision 0) or FP32
  * (precision 1, defect correction: residual, update and norms stay FP64; precision 2 also
- * reads the matrix and the factors from 16-bit block-scaled copies), the update, and the
+ * reads the matrix and the factors from 16-bit block-scaled copies and keeps the Krylov basis
+ * in FP16), the update, and the
  * CFL control (adaptive as adaptCourantNum_, src/SolverImplicit.cpp:530-550, or the additive
  * geometric ramp).  history (may be NULL): [n][19] = L2[5] and max[5] of the Dt/V-scaled
  * right-hand side (the max is what the reference logs, Q10), CFL used, CFL after the step,
