@@ -98,11 +98,12 @@ WORKLOADS = {
                                 train=(1, 32), test=(2, 8), data_iters=1500, eval_iters=1500,
                                 train_steps=3000, batch=8192,
                                 opts=dict(solver_type=0, local_time_step=1, courant_num=0.8)),
-    # warm-started FP32-system implicit sweep against the plain FP64 solver: 60x30x60-hex Gaussian
-    # box (648,000 tets); the warm start is trained on 16 conditions (seed 1) solved by a
-    # batched FP32-system implicit context; 6 held-out conditions (seed 2) are solved to the
-    # same absolute residual (1e-8 of the freestream start's first residual) by the plain FP64
-    # solver from the freestream and by the FP32-system solver from the prediction
+    # warm-started FP32-system implicit sweep (precision 2) against the plain FP64 solver:
+    # 60x30x60-hex Gaussian box (648,000 tets); the warm start is trained on 16 conditions
+    # (seed 1) solved by a batched implicit context; 6 held-out conditions (seed 2) are solved
+    # to the same absolute residual (1e-8 of the freestream start's first residual) by the
+    # plain FP64 solver from the freestream, and by the FP32-system solver with the production
+    # linear tolerance from the freestream and from the prediction
     "production_gauss_648k": dict(kind="production", mesh=("gauss", 60, 30, 60, 1.05),
                                   train=(1, 16), test=(2, 6), data_steps=200, max_steps=300,
                                   train_steps=5000, batch=8192,
@@ -110,7 +111,7 @@ WORKLOADS = {
                                             linear_solver=1, linear_solver_tol=1e-2,
                                             linear_solver_max_iter=300, gmres_restart=30,
                                             cfl_ramp_steps=50, cfl_ramp_start=10.0,
-                                            cfl_ramp_end=1000.0, precision=1)),
+                                            cfl_ramp_end=1000.0, precision=2)),
     # same scheme on the 200x60x30-hex channel (2.16M tets), Mach 0.84
     "explicit_bump_2m": dict(kind="explicit", mesh=("bump", 200, 60, 30, 0.08),
                              opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
@@ -583,10 +584,17 @@ def run_production(args, wl, torch, mesh, clocks):
         F64 = c64.wall_force()
         U64 = c64.get_state()
         c64.close()
-        # production settings: from a predicted field the CFL ramp starts at 100 (10 steps to
-        # 1000), and the linear solves stop at 1e-1 (the outer rate is set by the first-order
-        # Jacobian, so 1e-2 oversolves: on the 2.16M-cell channel 1e-1 converges to the same
-        # answer in 15.5 s instead of 22.4 s)
+        # production settings: the linear solves stop at 1e-1 (the outer rate is set by the
+        # first-order Jacobian, so 1e-2 oversolves: on the 2.16M-cell channel 1e-1 converges to
+        # the same answer 1.4x sooner); from a predicted field the CFL ramp starts at 100 (10
+        # steps to 1000)
+        q = 0.5 * float(np.sum(mach ** 2))
+        cc = lib.Context(mesh, lib.default_options(**dict(o32, freestream_mach=tuple(mach),
+                                                          linear_solver_tol=0.1)))
+        sc, tc, _, rc_, _ = _solve_to(cc, target, wl["max_steps"])
+        Fc = cc.wall_force()
+        Uc = cc.get_state()
+        cc.close()
         c32 = lib.Context(mesh, lib.default_options(**dict(o32, freestream_mach=tuple(mach),
                                                            cfl_ramp_start=100.0,
                                                            cfl_ramp_steps=10,
@@ -596,9 +604,12 @@ def run_production(args, wl, torch, mesh, clocks):
         F32 = c32.wall_force()
         U32 = c32.get_state()
         c32.close()
-        q = 0.5 * float(np.sum(mach ** 2))
         rows.append(dict(mach=[float(x) for x in mach], fp64_steps=s64, fp64_seconds=t64,
-                         fp64_converged=bool(r64 <= target), warm_steps=s32, warm_seconds=t32,
+                         fp64_converged=bool(r64 <= target),
+                         cold_steps=sc, cold_seconds=tc, cold_converged=bool(rc_ <= target),
+                         cold_force_coefficient_abs_diff=float(np.abs(Fc - F64).max() / q),
+                         cold_state_rel_l2_diff=float(np.linalg.norm(Uc - U64) / np.linalg.norm(U64)),
+                         warm_steps=s32, warm_seconds=t32,
                          warm_converged=bool(r32 <= target), prediction_used=used,
                          force_coefficient_abs_diff=float(np.abs(F32 - F64).max() / q),
                          state_rel_l2_diff=float(np.linalg.norm(U32 - U64) / np.linalg.norm(U64))))
@@ -607,11 +618,16 @@ def run_production(args, wl, torch, mesh, clocks):
     t_fp64 = sum(r["fp64_seconds"] for r in rows)
     t_warm = sum(r["warm_seconds"] for r in rows)
     warm_steps = sum(r["warm_steps"] for r in rows)
+    t_cold = sum(r["cold_seconds"] for r in rows)
     # solves/hour counts converged solves only (the wall time of every run is charged)
     n64 = sum(r["fp64_converged"] for r in rows)
     n32 = sum(r["warm_converged"] for r in rows)
+    ncold = sum(r["cold_converged"] for r in rows)
     sph64 = 3600.0 * n64 / t_fp64
     sph32 = 3600.0 * n32 / t_warm
+    sphc = 3600.0 * ncold / t_cold
+    same_cold = [r for r in rows if r["fp64_converged"] and r["cold_converged"]
+                 and r["cold_state_rel_l2_diff"] < 1e-6]
     all_conv = all(r["fp64_converged"] and r["warm_converged"] for r in rows)
     # the same steady state as the plain solver (the scheme has several at some conditions)
     same = [r for r in rows if r["fp64_converged"] and r["warm_converged"]
@@ -622,7 +638,8 @@ def run_production(args, wl, torch, mesh, clocks):
             "value": nc * warm_steps / t_warm, "unit": METRIC, "n_gpus": 1,
             "steps": warm_steps, "warmup": 0, "ms_per_step": t_warm / warm_steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 system / f64 residual and update", "data": "synthetic",
+            "dtype": "f32 system stored as fp16 blocks, fp16 Krylov basis / f64 residual and "
+                     "update", "data": "synthetic",
             "config": {"workload": args.workload, "cells": nc,
                        "train_conditions_converged": len(train), "test_conditions": n,
                        "parallelism": "replicas1",
@@ -633,6 +650,10 @@ def run_production(args, wl, torch, mesh, clocks):
                                                         "plain_fp64": n64, "of": n},
                                           "same_steady_state_as_plain": len(same),
                                           "all_converged": all_conv,
+                                          "cold_fp32_system": sphc,
+                                          "cold_ratio": sphc / sph64 if sph64 else None,
+                                          "cold_converged": ncold,
+                                          "cold_same_steady_state_as_plain": len(same_cold),
                                           "target": "1e-8 x the freestream start's first "
                                                     "residual L2, per condition"},
             "max_force_coefficient_abs_diff": max(r["force_coefficient_abs_diff"] for r in rows),

@@ -149,14 +149,21 @@ void enqueue_ilu_factor(const Sys<T>& S) {
   const SoaMesh& M = c->soa;
   // the factors overwrite a copy: the Krylov products need the unfactored matrix
   cudaMemcpyAsync(S.LU, S.A, (size_t)125 * S.nc * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
+  // per stage: the factorisation of its rows, then the inverses of their diagonal blocks (a
+  // separate kernel keeps the factorisation's registers free of the 5x10 elimination array)
   for (int k = 0; k < M.n_stages; ++k) {
     const int n = M.stage_off[k + 1] - M.stage_off[k];
-    if (c->imp.use_colour_ranges)
+    if (c->imp.use_colour_ranges) {
       ilu_factor_kernel<T, true><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, nullptr, n, nullptr, S.LU,
                                                                 S.Dinv, M.stage_off[k]);
-    else
+      ilu_invert_kernel<T, true><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, nullptr, n, S.LU, S.Dinv,
+                                                                M.stage_off[k]);
+    } else {
       ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
                                                           n, c->imp.ilu_pos, S.LU, S.Dinv);
+      ilu_invert_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
+                                                          n, S.LU, S.Dinv);
+    }
   }
   if (S.packed) {
     enqueue_pack(S, S.LU, 1, 4, c->imp.LU16, c->imp.LUs);
@@ -290,7 +297,7 @@ int precond_setup(const Sys<T>& S) {
   prof_begin(c, PROF_ILU_FACTOR);
   IMP_TRY(c, cudaGraphLaunch(c->imp.factor_graph, S.s));
   prof_end(c, PROF_ILU_FACTOR);
-  c->launches += c->soa.n_stages;
+  c->launches += 2 * c->soa.n_stages + (S.packed ? 2 : 0);
   return BES_OK;
 }
 

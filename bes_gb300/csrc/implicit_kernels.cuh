@@ -30,6 +30,11 @@ __device__ __forceinline__ T ellc(const T* A, int s, int q, int nc, int i) {
   return A[(int64_t)(s * 25 + q) * nc + i];
 }
 
+// a[k] for a runtime k in [0, 4) without indexing the array (keeps it in registers)
+__device__ __forceinline__ int sel4(const int* a, int k) {
+  return k == 0 ? a[0] : (k == 1 ? a[1] : (k == 2 ? a[2] : a[3]));
+}
+
 // 5x5 inverse by Gauss-Jordan elimination with partial pivoting.
 template <class T>
 __device__ __forceinline__ void inv5(const T* a, T* inv) {
@@ -327,8 +332,8 @@ __global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_
     // A_ik -= L_ij U_jk for every k in row i's pattern with pos(k) > pos(j) and (j,k) present
 #pragma unroll 1
     for (int kk = -1; kk < 4; ++kk) {
-      const int col = kk < 0 ? i : nbr[kk];
-      if (kk >= 0 && (col < 0 || pn[kk] <= pj)) continue;
+      const int col = kk < 0 ? i : sel4(nbr, kk);
+      if (kk >= 0 && (col < 0 || sel4(pn, kk) <= pj)) continue;
       int sj = -1;
       for (int q = 0; q < 4; ++q)
         if (m.adj[q * nc + j] == col) sj = q;
@@ -345,9 +350,20 @@ __global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_
         }
     }
   }
+}
+
+// inverse of the factored diagonal block of each row of a stage (after ilu_factor_kernel)
+template <class T, bool RANGE = false>
+__global__ void __launch_bounds__(128) ilu_invert_kernel(DevMesh m, const int32_t* __restrict__ rows,
+                                                         int nrows, const T* __restrict__ A,
+                                                         T* __restrict__ Dinv, int r0 = 0) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows) return;
+  const int nc = m.nc;
+  const int i = RANGE ? r0 + t : rows[t];
   T D[25], inv[25];
 #pragma unroll
-  for (int q = 0; q < 25; ++q) D[q] = ell(A, 0, q, nc, i);
+  for (int q = 0; q < 25; ++q) D[q] = ellc(A, 0, q, nc, i);
   inv5(D, inv);
 #pragma unroll
   for (int q = 0; q < 25; ++q) Dinv[(int64_t)q * nc + i] = inv[q];
