@@ -317,14 +317,21 @@ __global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_
         j = nbr[t];
         pj = pn[t];
       }
-    T L[25];
+    // blocks are loaded into registers before any store: A is read and written through one
+    // pointer, so loads issued after a store could not be batched or reused
+    T L[25], Ais[25], Dj[25];
+#pragma unroll
+    for (int q = 0; q < 25; ++q) {
+      Ais[q] = ellc(A, 1 + s, q, nc, i);
+      Dj[q] = Dinv[(int64_t)q * nc + j];
+    }
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
       for (int c = 0; c < 5; ++c) {
         T acc = T(0);
 #pragma unroll
-        for (int k = 0; k < 5; ++k) acc += ell(A, 1 + s, r * 5 + k, nc, i) * Dinv[(int64_t)(k * 5 + c) * nc + j];
+        for (int k = 0; k < 5; ++k) acc += Ais[r * 5 + k] * Dj[k * 5 + c];
         L[r * 5 + c] = acc;
       }
 #pragma unroll
@@ -339,15 +346,23 @@ __global__ void __launch_bounds__(128) ilu_factor_kernel(DevMesh m, const int32_
         if (m.adj[q * nc + j] == col) sj = q;
       if (sj < 0) continue;
       const int dst = kk < 0 ? 0 : 1 + kk;
+      T U[25], Ad[25];
+#pragma unroll
+      for (int q = 0; q < 25; ++q) {
+        U[q] = ellc(A, 1 + sj, q, nc, j);
+        Ad[q] = ellc(A, dst, q, nc, i);
+      }
 #pragma unroll
       for (int r = 0; r < 5; ++r)
 #pragma unroll
         for (int c = 0; c < 5; ++c) {
           T acc = T(0);
 #pragma unroll
-          for (int k = 0; k < 5; ++k) acc += L[r * 5 + k] * ell(A, 1 + sj, k * 5 + c, nc, j);
-          ell(A, dst, r * 5 + c, nc, i) -= acc;
+          for (int k = 0; k < 5; ++k) acc += L[r * 5 + k] * U[k * 5 + c];
+          Ad[r * 5 + c] -= acc;
         }
+#pragma unroll
+      for (int q = 0; q < 25; ++q) ell(A, dst, q, nc, i) = Ad[q];
     }
   }
 }
