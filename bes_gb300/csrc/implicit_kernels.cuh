@@ -612,14 +612,22 @@ static __global__ void __launch_bounds__(256) spmv_packed_kernel(
   const int nc = m.nc;
   if (i >= nc) return;
   float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  // branch-free, so that every slot's loads can be in flight together: the block of a slot
+  // without a neighbour is zero (boundary face, or the empty fourth slot of a triangle), and
+  // the row's own values stand in for the missing neighbour's, adding exactly 0
+  int jn[5];
+  jn[0] = i;
+#pragma unroll
+  for (int s = 1; s < 5; ++s) {
+    const int j = m.adj[(s - 1) * nc + i];
+    jn[s] = j >= 0 ? j : i;
+  }
 #pragma unroll
   for (int s = 0; s < 5; ++s) {
-    const int j = s == 0 ? i : m.adj[(s - 1) * nc + i];
-    if (j < 0) continue;
     const float sc = S[(int64_t)s * nc + i];
     float xs[5], a[26];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) xs[v] = sc * x[(int64_t)j * 5 + v];
+    for (int v = 0; v < 5; ++v) xs[v] = sc * x[(int64_t)jn[s] * 5 + v];
     load_packed(H, s, nc, i, a);
 #pragma unroll
     for (int r = 0; r < 5; ++r)
@@ -645,9 +653,13 @@ __global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
   float acc[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
+  // the four neighbour ids first (one round trip), then the qualifying slots
+  int jn[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) jn[s] = m.adj[s * nc + i];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
-    const int j = m.adj[s * nc + i];
+    const int j = jn[s];
     const bool lower = LOWER && j >= 0 && j < r0;
     const bool upper = UPPER && j >= r1;
     if (!lower && !upper) continue;
