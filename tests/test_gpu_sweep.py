@@ -98,7 +98,7 @@ def test_sweep_run_stops_each_condition_at_its_drop():
     ctx.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_implicit_batch_matches_single_condition_runs(precision):
     """Implicit batches step the conditions one after another through shared implicit
     buffers; every condition, with its own adaptive CFL, matches its own context."""
