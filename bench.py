@@ -112,6 +112,15 @@ WORKLOADS = {
                                             linear_solver_max_iter=300, gmres_restart=30,
                                             cfl_ramp_steps=50, cfl_ramp_start=10.0,
                                             cfl_ramp_end=1000.0, precision=2)),
+    # production form at scale: the Gaussian-bump box at 200x100x200 hexes (24.0M tets), 16
+    # conditions (seed 3) in one batched implicit context (precision 2, the benchmark's
+    # GMRES settings); a throughput measurement of whole batched steps, not converged solves
+    "implicit_gauss_24m_16": dict(kind="scale", mesh=("gauss", 200, 100, 200, 1.05), conds=(3, 16),
+                                  opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
+                                            linear_solver=1, linear_solver_tol=1e-2,
+                                            linear_solver_max_iter=300, gmres_restart=30,
+                                            cfl_ramp_steps=50, cfl_ramp_start=10.0,
+                                            cfl_ramp_end=1000.0, precision=2)),
     # same scheme on the 200x60x30-hex channel (2.16M tets), Mach 0.84
     "explicit_bump_2m": dict(kind="explicit", mesh=("bump", 200, 60, 30, 0.08),
                              opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
@@ -246,7 +255,7 @@ def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    if wl["kind"] in ("implicit", "production"):
+    if wl["kind"] in ("implicit", "production", "scale"):
         steps = max(1, min(args.steps, 3))
         base = implicit_cpu_baseline(wl, steps=steps)
         value = base["value"]
@@ -661,6 +670,56 @@ def run_production(args, wl, torch, mesh, clocks):
             "clocks": clk}
 
 
+def run_scale(args, wl, torch, mesh, clocks):
+    """Batched implicit steps of many conditions on a large mesh: one step = one implicit step
+    of every condition (stepped one after another through the shared implicit buffers); value =
+    conditions x cells x steps / event-timed device time.  Reports the device memory the
+    context holds and its set-up time (host mesh build, renumbering, upload)."""
+    from bes_gb300 import lib, meshgen
+    seed, n = wl["conds"]
+    machs = np.array([meshgen.freestream_mach_vector(*c)
+                      for c in meshgen.sample_conditions(n, seed)])
+    free0, total = torch.cuda.mem_get_info()
+    t0 = time.perf_counter()
+    ctx = lib.Context(mesh, lib.default_options(**wl["opts"]), machs=machs)
+    t_setup = time.perf_counter() - t0
+    ctx.implicit_steps(args.warmup)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    ext = torch.cuda.ExternalStream(ctx.stream_handle)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    c0 = ctx.counters()
+    hist = []
+    clocks.start()
+    for k in range(args.steps):
+        starts[k].record(ext)
+        hist.append(ctx.implicit_steps(1)[0])
+        ends[k].record(ext)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    c1 = ctx.counters()
+    dev_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
+    hist = np.array(hist)  # [steps, n, 19]
+    nc = ctx.n_cells
+    ctx.close()
+    value = n * nc * args.steps / (dev_ms / 1e3)
+    return {"metric": METRIC, "metric_full": METRIC_FULL, "value": value, "unit": METRIC,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 system stored as fp16 blocks, fp16 Krylov basis / f64 residual and "
+                     "update", "data": "synthetic",
+            "config": {"workload": args.workload, "cells": nc, "conditions": n,
+                       "parallelism": "replicas1",
+                       "l2": "inputs larger than L2 (a step streams tens of GB)",
+                       "linear_iterations_per_condition_step": float(hist[:, :, 12].mean()),
+                       "device_memory_gb": (free0 - free1) / 1e9,
+                       "device_memory_total_gb": total / 1e9,
+                       "setup_seconds": t_setup},
+            "e2e": None, "gpu_launches": c1["launches"] - c0["launches"], "clocks": clk}
+
+
 def run_converge(args, wl, ctx, max_steps: int, drop: float = 1e-8):
     """Implicit steps until the L2 of the unscaled residual (all variables) falls by `drop`
     relative to the first step; returns steps, device-synchronous wall time and the history."""
@@ -720,8 +779,9 @@ def main():
     from bes_gb300 import lib
     nbuild.build()
     mesh = make_mesh(wl["mesh"])
-    if wl["kind"] in ("warmstart", "production"):
-        fn = run_warmstart if wl["kind"] == "warmstart" else run_production
+    if wl["kind"] in ("warmstart", "production", "scale"):
+        fn = {"warmstart": run_warmstart, "production": run_production,
+              "scale": run_scale}[wl["kind"]]
         line = fn(args, wl, torch, mesh, ClockSampler(local_rank))
         if rank == 0:
             print(json.dumps(line))
