@@ -191,6 +191,144 @@ static bool build_mesh(const double* X, const int64_t* tets, int64_t nc, const i
   return true;
 }
 
+// Mesh::readGmsh for a 2-D file (src/Mesh.cpp:235-426): boundary lines (FaceGmshOne,
+// MeshGmsh.cpp:22-42: centre = midpoint, normal = (y1 - y0, x0 - x1), area = its length) are
+// created first; triangle c's edges are (v0,v1), (v1,v2), (v2,v0); an edge met for the first
+// time becomes an internal face with the triangle's vertex order (normal out of the triangle),
+// a boundary line met by a triangle is flipped if its normal opposes the triangle's outward
+// normal (MeshMath::computeTwoDimOutwardNormal, MeshCommon.cpp:60-67) and gets the triangle
+// as owner, an internal edge met again gets it as neighbour.  Cells: area
+// (ElementGmshTwo::computeVolume, MeshGmsh.cpp:76-82), centroid = vertex mean (:84-93), then
+// the vectors, weights and projected lengths of the 3-D path over three faces; the MUSCL
+// lookup (Q13) resolves face 0 to the last slot, 2.  z is read as 0 throughout.
+static bool build_mesh_2d(const double* X, const int64_t* tris, int64_t nc, const int64_t* lines,
+                          const int32_t* btags, int64_t nb, int muscl_exact, Mesh& M, char* err) {
+  M.dim = 2;
+  M.nfc = 3;
+  std::unordered_map<std::array<int64_t, 3>, int64_t, KeyHash> key2face;
+  key2face.reserve((size_t)(2 * nc + nb));
+  auto key_of = [](int64_t a, int64_t b) {
+    return std::array<int64_t, 3>{a < b ? a : b, a < b ? b : a, -1};
+  };
+  auto make_face = [&](int64_t a, int64_t b, int kind) -> int64_t {
+    const int64_t id = (int64_t)M.kind.size();
+    M.kind.push_back(kind);
+    const double Sx = X[b * 3 + 1] - X[a * 3 + 1];
+    const double Sy = X[a * 3] - X[b * 3];
+    const double len = std::sqrt(sq(Sx) + sq(Sy));
+    M.center.push_back(0.5 * (X[a * 3] + X[b * 3]));
+    M.center.push_back(0.5 * (X[a * 3 + 1] + X[b * 3 + 1]));
+    M.center.push_back(0.0);
+    M.S.push_back(Sx);
+    M.S.push_back(Sy);
+    M.S.push_back(0.0);
+    M.nhat.push_back(Sx / len);
+    M.nhat.push_back(Sy / len);
+    M.nhat.push_back(0.0);
+    M.area.push_back(len);
+    M.owner.push_back(-1);
+    M.neigh.push_back(-1);
+    return id;
+  };
+  for (int64_t b = 0; b < nb; ++b) {
+    const int kind = btags[b] == 1 ? FACE_SLIP_WALL : (btags[b] == 2 ? FACE_FREESTREAM : -1);
+    if (kind < 0) {
+      std::snprintf(err, 256, "boundary line %lld has unknown tag %d", (long long)b, btags[b]);
+      return false;
+    }
+    key2face[key_of(lines[b * 2], lines[b * 2 + 1])] = make_face(lines[b * 2], lines[b * 2 + 1], kind);
+  }
+  M.nc = nc;
+  M.cface.assign(nc * 4, -1);
+  M.cadj.assign(nc * 4, -1);
+  for (int64_t c = 0; c < nc; ++c) {
+    const int64_t* p = &tris[c * 3];
+    for (int m = 0; m < 3; ++m) {
+      const int64_t a = p[m], b = p[(m + 1) % 3];
+      const auto k = key_of(a, b);
+      auto it = key2face.find(k);
+      int64_t f;
+      if (it == key2face.end()) {
+        f = make_face(a, b, FACE_INTERNAL);
+        key2face[k] = f;
+        M.owner[f] = c;
+      } else {
+        f = it->second;
+        if (M.kind[f] != FACE_INTERNAL) {
+          const double ox = X[b * 3 + 1] - X[a * 3 + 1];
+          const double oy = -X[b * 3] + X[a * 3];
+          if (M.S[f * 3] * ox + M.S[f * 3 + 1] * oy < 0)
+            for (int d = 0; d < 2; ++d) {
+              M.S[f * 3 + d] = -M.S[f * 3 + d];
+              M.nhat[f * 3 + d] = -M.nhat[f * 3 + d];
+            }
+          M.owner[f] = c;
+          M.neigh[f] = -1;
+        } else {
+          M.neigh[f] = c;
+        }
+      }
+      M.cface[c * 4 + m] = f;
+    }
+  }
+  M.nf = (int64_t)M.kind.size();
+  for (int64_t f = 0; f < M.nf; ++f) {
+    if (M.owner[f] < 0) {
+      std::snprintf(err, 256, "face %lld has no owner cell", (long long)f);
+      return false;
+    }
+    if (M.kind[f] == FACE_INTERNAL && M.neigh[f] < 0) {
+      std::snprintf(err, 256, "internal edge %lld has a single cell (missing boundary line)",
+                    (long long)f);
+      return false;
+    }
+  }
+  M.vol.assign(nc, 0);
+  M.centroid.assign(nc * 3, 0);
+  M.rvec.assign(nc * 12, 0);
+  M.weight.assign(nc * 4, 0);
+  M.plen.assign(nc * 3, 0);
+  M.muscl_slot.assign(nc * 4, 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    const double* v0 = &X[tris[c * 3] * 3];
+    const double* v1 = &X[tris[c * 3 + 1] * 3];
+    const double* v2 = &X[tris[c * 3 + 2] * 3];
+    M.vol[c] = 0.5 * std::fabs((v0[0] - v1[0]) * (v2[1] - v1[1]) - (v2[0] - v1[0]) * (v0[1] - v1[1]));
+    for (int d = 0; d < 2; ++d) M.centroid[c * 3 + d] = (v0[d] + v1[d] + v2[d]) / 3;
+    for (int m = 0; m < 3; ++m) {
+      const int64_t f = M.cface[c * 4 + m];
+      for (int d = 0; d < 2; ++d)
+        M.rvec[c * 12 + m * 3 + d] = M.center[f * 3 + d] - M.centroid[c * 3 + d];
+    }
+  }
+  for (int64_t c = 0; c < nc; ++c) {
+    for (int m = 0; m < 3; ++m) {
+      const int64_t f = M.cface[c * 4 + m];
+      if (M.kind[f] == FACE_INTERNAL) M.cadj[c * 4 + m] = (M.owner[f] != c) ? M.owner[f] : M.neigh[f];
+    }
+    for (int m = 0; m < 3; ++m) {
+      const int64_t a = M.cadj[c * 4 + m];
+      if (a < 0) continue;
+      const int64_t f = M.cface[c * 4 + m];
+      double d1 = 0, d2 = 0;
+      for (int d = 0; d < 2; ++d) {
+        d1 += sq(M.centroid[c * 3 + d] - M.center[f * 3 + d]);
+        d2 += sq(M.centroid[a * 3 + d] - M.center[f * 3 + d]);
+      }
+      d1 = std::sqrt(d1);
+      d2 = std::sqrt(d2);
+      M.weight[c * 4 + m] = d2 / (d1 + d2);
+    }
+    for (int m = 0; m < 3; ++m)
+      for (int d = 0; d < 2; ++d) M.plen[c * 3 + d] += std::fabs(M.S[M.cface[c * 4 + m] * 3 + d]);
+    for (int d = 0; d < 2; ++d) M.plen[c * 3 + d] /= 2.0;
+    for (int m = 0; m < 3; ++m)
+      M.muscl_slot[c * 4 + m] = muscl_exact ? m : (M.cface[c * 4 + m] == 0 ? 2 : 0);
+    M.muscl_slot[c * 4 + 3] = -1;
+  }
+  return true;
+}
+
 struct Oracle {
   Mesh M;
   Gas g;
@@ -272,7 +410,7 @@ static void compute_gradient(Oracle& O, const double* U) {
   for (int64_t c = 0; c < M.nc; ++c) {
     double* G = &O.G[c * 15];
     const double* ui = &U[c * 5];
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < M.nfc; ++m) {
       const int64_t f = M.cface[c * 4 + m];
       const double* S = &M.S[f * 3];
       const int64_t nb = M.cadj[c * 4 + m];
@@ -316,7 +454,7 @@ static void compute_limiter(Oracle& O, const double* U) {
   O.phi.assign(M.nc * 5, 0);
 #pragma omp parallel for num_threads(O.threads)
   for (int64_t c = 0; c < M.nc; ++c) {
-    const double len = std::pow(M.vol[c], 1.0 / 3);
+    const double len = std::pow(M.vol[c], 1.0 / M.dim);
     const double eps = std::pow(O.o.venkat_k * len, 3.0 / 2.0);
     for (int v = 0; v < 5; ++v) {
       const double ui = U[c * 5 + v];
@@ -394,7 +532,7 @@ static void compute_residual(Oracle& O, const double* U) {
   O.R.assign(M.nc * 5, 0);
 #pragma omp parallel for num_threads(O.threads)
   for (int64_t c = 0; c < M.nc; ++c) {
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < M.nfc; ++q) {
       const int m = (int)O.cface_sorted[c * 4 + q];
       const int64_t f = M.cface[c * 4 + m];
       for (int v = 0; v < 5; ++v) {
@@ -586,7 +724,7 @@ static void implicit_step(Oracle& O, double* hist) {
   const int rep = O.o.jacobian_repeat;
 #pragma omp parallel for num_threads(O.threads)
   for (int64_t c = 0; c < M.nc; ++c) {
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < M.nfc; ++q) {
       const int m = (int)O.cface_sorted[c * 4 + q];
       const int64_t f = M.cface[c * 4 + m];
       const int64_t o = M.owner[f], nb = M.neigh[f];
@@ -643,7 +781,7 @@ static void implicit_step(Oracle& O, double* hist) {
     double r2[5] = {0, 0, 0, 0, 0};
     for (int64_t c = 0; c < M.nc; ++c) {
       double R[5] = {0, 0, 0, 0, 0};
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < M.nfc; ++q) {
         const int m = (int)O.cface_sorted[c * 4 + q];
         const int64_t f = M.cface[c * 4 + m];
         for (int v = 0; v < 5; ++v) {
@@ -688,8 +826,8 @@ struct bor_options {
 };
 
 void* bor_create(const double* nodes, int64_t nv, const int64_t* tets, int64_t nc,
-                 const int64_t* btris, const int32_t* btags, int64_t nb, const bor_options* op,
-                 char* errbuf) {
+                 const int64_t* btris, const int32_t* btags, int64_t nb, int32_t dim,
+                 const bor_options* op, char* errbuf) {
   (void)nv;
   bor::Oracle* O = new bor::Oracle();
   bor::Options& o = O->o;
@@ -719,15 +857,22 @@ void* bor_create(const double* nodes, int64_t nv, const int64_t* tets, int64_t n
   o.fs_frac = op->fs_frac;
   O->threads = op->threads > 0 ? op->threads : 1;
   O->g.init(o.gas_constant, o.gamma);
-  if (!bor::build_mesh(nodes, tets, nc, btris, btags, nb, o.muscl_exact, O->M, O->err)) {
+  const bool ok = dim == 2 ? bor::build_mesh_2d(nodes, tets, nc, btris, btags, nb,
+                                                 o.muscl_exact, O->M, O->err)
+                           : bor::build_mesh(nodes, tets, nc, btris, btags, nb, o.muscl_exact,
+                                             O->M, O->err);
+  if (!ok) {
     if (errbuf) std::snprintf(errbuf, 256, "%s", O->err);
     delete O;
     return nullptr;
   }
+  // per cell, the local faces in increasing face id (the order the reference's face loop adds
+  // them to a cell's residual); the empty slot of a triangle stays last
+  const int nfc = O->M.nfc;
   O->cface_sorted.resize(nc * 4);
   for (int64_t c = 0; c < nc; ++c) {
     int64_t idx[4] = {0, 1, 2, 3};
-    std::sort(idx, idx + 4, [&](int64_t a, int64_t b) {
+    std::sort(idx, idx + nfc, [&](int64_t a, int64_t b) {
       return O->M.cface[c * 4 + a] < O->M.cface[c * 4 + b];
     });
     for (int q = 0; q < 4; ++q) O->cface_sorted[c * 4 + q] = idx[q];

@@ -289,6 +289,8 @@ enum FaceKind { FACE_INTERNAL = 0, FACE_SLIP_WALL = 1, FACE_FREESTREAM = 2 };
 // Reference-semantics mesh (src/Mesh.cpp:95-636, src/MeshGmsh.cpp, src/Element.cpp).
 struct Mesh {
   int64_t nc = 0, nf = 0;
+  int dim = 3;  // 2: triangles, edges as faces, z ignored
+  int nfc = 4;  // faces per cell (3 for triangles: local slot 3 is empty, cface = cadj = -1)
   // faces in reference creation order
   std::vector<double> S, nhat, area, center;  // [nf*3], [nf*3], [nf], [nf*3]
   std::vector<int64_t> owner, neigh;          // neigh = -1 on boundary

@@ -70,7 +70,7 @@ def lib():
         I64 = ctypes.POINTER(ctypes.c_int64)
         L.bor_create.restype = P
         L.bor_create.argtypes = [D, ctypes.c_int64, I64, ctypes.c_int64, I64,
-                                 ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,
+                                 ctypes.POINTER(ctypes.c_int32), ctypes.c_int64, ctypes.c_int32,
                                  ctypes.POINTER(_Opts), ctypes.c_char_p]
         L.bor_destroy.argtypes = [P]
         L.bor_sizes.argtypes = [P, I64]
@@ -122,6 +122,8 @@ class Oracle:
     """One mesh + options; state kept in reference (file) numbering, cell-major AoS [nc,5]."""
 
     def __init__(self, mesh, **opts):
+        """mesh: tetrahedra [nc,4] with boundary triangles [nb,3], or triangles [nc,3] with
+        boundary lines [nb,2] (the reference's 2-D path)."""
         L = lib()
         self._keep = [np.ascontiguousarray(mesh.nodes, dtype=np.float64),
                       np.ascontiguousarray(mesh.tets, dtype=np.int64),
@@ -132,7 +134,8 @@ class Oracle:
         err = ctypes.create_string_buffer(256)
         self.h = L.bor_create(_d(nodes), nodes.shape[0], _i(tets), tets.shape[0], _i(btris),
                               btags.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                              btris.shape[0], ctypes.byref(self.opts), err)
+                              btris.shape[0], 2 if tets.shape[1] == 3 else 3,
+                              ctypes.byref(self.opts), err)
         if not self.h:
             raise ValueError("oracle mesh build failed: " + err.value.decode())
         sz = np.zeros(2, dtype=np.int64)

@@ -1,20 +1,25 @@
 """Triangle meshes (the reference's 2-D path) on the GPU.
 
 The explicit path is pinned to the reference's own 2-D run in test_gpu_explicit.py (residual
-history and final state within 1e-10).  The reference build cannot run its implicit solver on a
-2-D mesh (its linear-solver facade is sized for five conserved variables), so the implicit
-path on triangles is checked through properties: it converges to the steady state of the
+history and final state within 1e-10) and here against the oracle with a global time step.
+The reference build cannot run its implicit solver on a 2-D mesh (its linear-solver facade is
+sized for five conserved variables), so the implicit path on triangles is checked against the
+oracle's restatement (the same five-variable formulation with zero spanwise momentum, given
+the GPU's block-ILU(0) order) and through properties: it converges to the steady state of the
 explicit path (the same discrete residual R(U) = 0), the FP32 system tracks the FP64 one, and
-the spanwise momentum stays exactly zero.
+the spanwise momentum stays zero.
 
-Tolerances: steady states of the two solvers 1e-7 relative to the state's scale (both driven
-to a residual drop of 1e-11); FP32 defect correction against FP64 after 15 steps 1e-3.
+Tolerances: explicit 1e-10 (as the 3-D path); implicit steps against the oracle 1e-9 with equal
+linear-iteration counts (as the 3-D path); steady states of the two solvers 1e-7 relative to
+the state's scale (both driven to a residual drop of 1e-11); FP32 defect correction against
+FP64 after 15 steps 1e-3.
 """
 import numpy as np
 import pytest
 
 from bes_gb300 import meshgen
-from tests._gpu import context, rel_err
+from oracle import pyoracle
+from tests._gpu import context, hist_rel_err, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -64,3 +69,27 @@ def test_2d_fp32_defect_correction_tracks_fp64(precond):
     assert rel_err(c32.get_state(), c64.get_state()) <= 1e-3
     assert np.max(np.abs(np.log(h32[:, [0, 1, 2, 4]] / h64[:, [0, 1, 2, 4]]))) <= 0.05
     assert np.abs(c32.get_state()[:, 3]).max() <= 1e-13
+
+
+def test_2d_explicit_global_dt_matches_oracle():
+    mesh = meshgen.bump_channel_2d(24, 8, 0.05)
+    ctx = context(mesh, solver_type=0, local_time_step=0, courant_num=0.8, freestream_mach=MACH)
+    h = ctx.explicit_iterations(50)
+    O = pyoracle.Oracle(mesh, local_dt=0, cfl=0.8, mach=MACH)
+    ho = O.explicit_run(50)
+    assert hist_rel_err(h, ho) <= 1e-10
+    assert rel_err(ctx.get_state(), O.get_state()) <= 1e-10
+
+
+def test_2d_implicit_steps_match_oracle():
+    mesh = meshgen.bump_channel_2d(24, 8, 0.05)
+    ctx = _implicit(mesh, cfl_ramp_steps=8, cfl_ramp_end=500.0)
+    h = ctx.implicit_steps(10)
+    O = pyoracle.Oracle(mesh, solver=1, local_dt=1, cfl=10.0, mach=MACH, lin_precond=1,
+                        lin_tol=1e-2, lin_maxiter=300, lin_restart=30, ramp_steps=8,
+                        ramp_cfl0=10.0, ramp_cfl1=500.0)
+    O.set_ilu_order(ctx.ilu_order())
+    ho = O.implicit_run(10)
+    assert np.array_equal(h[:, 12], ho[:, 12])
+    assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
+    assert rel_err(ctx.get_state(), O.get_state()) <= 1e-9

@@ -18,7 +18,7 @@ def rel_err(a, b):
     return np.abs(a - b).max() / scale
 
 
-@pytest.mark.parametrize("case", G.CASES)
+@pytest.mark.parametrize("case", G.CASES + G.CASES_2D)
 def test_geometry_matches_reference(case):
     ref, info = G.load(case)
     if "geo_volume" not in ref:
@@ -32,7 +32,7 @@ def test_geometry_matches_reference(case):
         assert np.array_equal(geo[k].ravel(), ref["geo_" + k]), k
 
 
-@pytest.mark.parametrize("case", [c for c in G.CASES if c.startswith("explicit")])
+@pytest.mark.parametrize("case", [c for c in G.CASES if c.startswith("explicit")] + G.CASES_2D)
 def test_explicit_history_matches_reference(case):
     ref, info = G.load(case)
     O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
