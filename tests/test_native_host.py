@@ -120,6 +120,47 @@ def test_mesh_errors_are_reported():
         lib.host_geometry(bad2)
 
 
+def test_triangle_mesh_errors_are_reported():
+    m = meshgen.bump_channel_2d(8, 4, 0.08)
+    # an edge with one triangle and no boundary line
+    bad = meshgen.TetMesh(m.nodes, m.tets, m.btris[3:], m.btags[3:])
+    with pytest.raises(lib.BesError) as e:
+        lib.host_geometry(bad)
+    assert e.value.code == 4 and "one triangle" in str(e.value)
+    # a boundary line with an unknown tag
+    with pytest.raises(lib.BesError, match="unknown boundary tag"):
+        lib.host_geometry(meshgen.TetMesh(m.nodes, m.tets, m.btris, np.full_like(m.btags, 7)))
+
+
+def test_gmsh_reader_2d_rules(tmp_path):
+    """2-D files (largest physical-name dimension 2): lines are the boundary, triangles the
+    cells; a line after a triangle and a tetrahedron are rejected (Mesh::readGmsh reads the
+    boundary first and has no 3-D element in a 2-D problem)."""
+    m = meshgen.bump_channel_2d(4, 2, 0.08)
+    p = str(tmp_path / "m.msh")
+    meshgen.write_gmsh(m, p)
+    text = open(p).read()
+    head, rest = text.split("$Elements\n")
+    count, body = rest.split("\n", 1)
+    rows = body.split("$EndElements")[0].strip().split("\n")
+    nb = m.btris.shape[0]
+    # move the first boundary line behind the triangles
+    swapped = rows[1:nb] + rows[nb:] + rows[:1]
+    q = str(tmp_path / "late_line.msh")
+    with open(q, "w") as f:
+        f.write(head + "$Elements\n" + count + "\n" + "\n".join(swapped) + "\n$EndElements\n")
+    with pytest.raises(lib.BesError, match="boundary line listed after a triangle"):
+        lib.read_gmsh(q)
+    # a tetrahedron in the 2-D file
+    extra = f"{len(rows) + 1} 4 2 3 3 1 2 3 4"
+    r = str(tmp_path / "tet.msh")
+    with open(r, "w") as f:
+        f.write(head + "$Elements\n" + str(len(rows) + 1) + "\n" + "\n".join(rows + [extra])
+                + "\n$EndElements\n")
+    with pytest.raises(lib.BesError, match="tetrahedron in a 2D problem"):
+        lib.read_gmsh(r)
+
+
 @pytest.mark.parametrize("make", [lambda: meshgen.gaussian_box(6, 4, 6),
                                   lambda: meshgen.bump_channel_2d(12, 4, 0.08)],
                          ids=["tetrahedra", "triangles"])
