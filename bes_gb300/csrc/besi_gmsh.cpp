@@ -192,7 +192,8 @@ extern "C" int bes_options_from_besi(const char* path, bes_options* o, char* mes
       if (w < 0) return bad("MUSCL_FACE_VECTOR must be REFERENCE or EXACT");
       o->muscl_face_vector = w;
     } else if (key == "GMRES_RESTART") {  // additive
-      if (!num(0, x) || x < 1 || x > 200) return bad("GMRES_RESTART must be 1..200");
+      // the Gram-Schmidt kernels take the basis size as a compile-time constant, up to 32
+      if (!num(0, x) || x < 1 || x > 32) return bad("GMRES_RESTART must be 1..32");
       o->gmres_restart = (int32_t)x;
     } else if (key == "PRECISION") {  // additive
       const int w = word({"FP64", "MIXED", "MIXED_PACKED"});

@@ -214,6 +214,7 @@ SAVE_INTERVAL = 10
     assert o.linear_solver_tol == 1e-2 and o.number_of_time_step == 7
     # untouched defaults (src/Config.cpp:73-114)
     assert o.venkatakrishnan_factor == 5.0 and o.harten_correction_limit == 0.05
+    assert o.gas_constant == 287.0 and o.specific_heat_ratio == 1.4
     assert o.precision == 0
 
 
@@ -222,11 +223,11 @@ def test_besi_precision_key(word, value):
     with tempfile.TemporaryDirectory() as d:
         o, _ = lib.options_from_besi(_write(d, f"PRECISION = {word}\n"))
     assert o.precision == value
-    assert o.gas_constant == 287.0 and o.specific_heat_ratio == 1.4
 
 
 @pytest.mark.parametrize("line", ["NOT_A_KEY = 1", "SOLVER_TYPE = SEMI", "FLUX_SCHEME = AUSM",
-                                  "FREESTREAM_MACH = 0.5, 0"])
+                                  "FREESTREAM_MACH = 0.5, 0", "GMRES_RESTART = 33",
+                                  "PRECISION = FP16"])
 def test_besi_parser_is_strict(line):
     with tempfile.TemporaryDirectory() as d:
         p = _write(d, "MESH_FORMAT = GMSH\n" + line + "\n")
