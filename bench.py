@@ -324,6 +324,26 @@ KERNEL_NAMES = {
     "spmv": {2: "spmv_packed_kernel", 1: "spmv_kernel", 0: "spmv_kernel"}}
 
 
+# FP64 floating-point operations per unit of the explicit path, counted: the fluxes by
+# instantiating the GPU's flux templates on a counting scalar (tests/opcount), the cell sweep
+# and the update per loop from their source (add, sub and mul count 1 each; the divisions and
+# square roots, 5 per cell and stage and 4 + 3 per face, come on top)
+FLOPS_PER_CELL_STAGE = 646  # cell sweep 614 (gradient 184, 1/V 15, limiter 370, MUSCL 45), update 32
+FLOPS_PER_CELL_DT = 33      # local time step, once per iteration
+FLOPS_PER_FACE_STAGE = 186  # Roe flux 181 + flux x area 5 (boundary faces need fewer)
+
+
+def explicit_fp64_work(nc: int, nf: int, cell_updates_per_s: float, n_stage: int = 4) -> dict:
+    """Counted FP64 work of one explicit iteration per cell and the rate it was done at."""
+    per_iter = (nc * (n_stage * FLOPS_PER_CELL_STAGE + FLOPS_PER_CELL_DT)
+                + nf * n_stage * FLOPS_PER_FACE_STAGE)
+    per_cell = per_iter / nc
+    return {"flops_per_cell_update": per_cell,
+            "achieved_tflops": cell_updates_per_s * per_cell / 1e12,
+            "note": "add/sub/mul counted once each (divisions and square roots on top); the "
+                    "cell sweep and the face flux are FP64-issue bound on this GPU"}
+
+
 def implicit_leg(args, torch, ctx, steps, warmup, flush, with_e2e):
     """warm-up, then `steps` timed implicit steps (events on the library stream around each
     step, L2 flushed before each); returns timing, history and the kernel-category profile."""
@@ -898,7 +918,8 @@ def main():
                        "l2": "flushed before every timed step (256 MB write)"},
             "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": 40 * nc * ncond,
                     "d2h_bytes_per_step": (40 * nc + 80) * ncond + 4},
-            "gpu_launches": 14 * args.steps, "roofline": roof, "clocks": clk}
+            "gpu_launches": 14 * args.steps, "roofline": roof,
+            "fp64_work": explicit_fp64_work(nc, nf, value / world), "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl, mesh, mach=None if machs is None else machs[0])
     ctx.close()

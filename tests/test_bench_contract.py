@@ -73,3 +73,18 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2
+
+
+def test_explicit_fp64_work_uses_the_counted_flops():
+    """The explicit line's FP64 work figure: the per-face constant is the counted Roe flux (add
+    and mul) plus the five area products, and the per-cell-update figure follows from it."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from tests.test_flux_opcount import EXPECTED
+    roe = EXPECTED["roe"]
+    assert bench.FLOPS_PER_FACE_STAGE == roe["add"] + roe["mul"] + 5
+    w = bench.explicit_fp64_work(72000, 148000, 1e8)
+    per_cell = (72000 * (4 * bench.FLOPS_PER_CELL_STAGE + bench.FLOPS_PER_CELL_DT)
+                + 148000 * 4 * bench.FLOPS_PER_FACE_STAGE) / 72000
+    assert w["flops_per_cell_update"] == pytest.approx(per_cell)
+    assert w["achieved_tflops"] == pytest.approx(1e8 * per_cell / 1e12)
