@@ -40,7 +40,8 @@ def _headers():
 def _compile(src: str, obj: str, verbose_ptxas: bool) -> str:
     # host code without FMA contraction, so that x86 and Arm hosts compute the same geometry
     flags = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-             "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
+             "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread",
+             "-I" + os.path.join(ROOT, "include")]
     if src.endswith(".cu"):
         flags += ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
         if verbose_ptxas:
@@ -74,7 +75,7 @@ def build(force: bool = False, verbose_ptxas: bool = False, quiet: bool = True) 
     if (jobs or not os.path.exists(LIB)
             or max(os.path.getmtime(o) for o in objs) > os.path.getmtime(LIB)):
         tmp = LIB + f".tmp{os.getpid()}"
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-pthread", "-o", tmp] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

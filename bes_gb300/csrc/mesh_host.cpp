@@ -18,6 +18,7 @@
 #include <cstring>
 #include <deque>
 #include <numeric>
+#include <thread>
 
 namespace bes {
 
@@ -27,6 +28,35 @@ constexpr int kBalancedColours = 5;
 namespace {
 
 const int kTetFace[4][3] = {{0, 2, 1}, {1, 2, 3}, {0, 3, 2}, {0, 1, 3}};
+
+// body(begin, end) over [0, n) in contiguous chunks on up to 16 threads.  Every index is
+// handled by exactly one call, so a loop whose iterations write disjoint elements and read
+// only what earlier loops wrote gives the serial loop's result.  A chunk whose thread cannot
+// be started runs on the calling thread.
+template <class F>
+void parallel_for(int64_t n, F&& body) {
+  const int64_t kMinChunk = 1 << 15;
+  const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+  const int64_t nt = std::min<int64_t>({hw, 16, (n + kMinChunk - 1) / kMinChunk});
+  if (nt <= 1) {
+    if (n > 0) body((int64_t)0, n);
+    return;
+  }
+  const int64_t chunk = (n + nt - 1) / nt;
+  std::vector<std::thread> threads;
+  threads.reserve((size_t)nt);
+  for (int64_t t = 1; t < nt; ++t) {
+    const int64_t b = t * chunk, e = std::min(n, b + chunk);
+    if (b >= e) break;
+    try {
+      threads.emplace_back([&body, b, e] { body(b, e); });
+    } catch (...) {
+      body(b, e);
+    }
+  }
+  body((int64_t)0, std::min(n, chunk));
+  for (auto& th : threads) th.join();
+}
 
 inline void cross_ref(const double* a, const double* b, const double* c, double* r) {
   // (c - b) x (a - b)  (MeshMath::crossProduct, src/MeshCommon.cpp:77-96)
@@ -102,7 +132,8 @@ inline void sort3(int64_t* k) {
 // map is keyed by face id 0 for every face, so face 0 resolves to the cell's last slot).
 void cell_links(RefMesh& M, int nfc, bool muscl_exact) {
   const int64_t nc = M.nc;
-  for (int64_t c = 0; c < nc; ++c) {
+  parallel_for(nc, [&](int64_t c0, int64_t c1) {
+  for (int64_t c = c0; c < c1; ++c) {
     for (int m = 0; m < nfc; ++m) {
       const int64_t f = M.cface[c * 4 + m];
       if (M.kind[f] == KIND_INTERNAL) M.cadj[c * 4 + m] = (M.owner[f] != c) ? M.owner[f] : M.neigh[f];
@@ -129,6 +160,7 @@ void cell_links(RefMesh& M, int nfc, bool muscl_exact) {
       M.muscl_slot[c * 4 + m] =
           (int8_t)(muscl_exact ? m : (M.cface[c * 4 + m] == 0 ? nfc - 1 : 0));
   }
+  });
 }
 
 // Triangle meshes (Mesh::readGmsh, src/Mesh.cpp:235-426; MeshGmsh.cpp:22-42, 71-93): boundary
@@ -246,7 +278,8 @@ bool build_ref_mesh_2d(const double* X, int64_t nv, const int64_t* blines, const
   M.weight.assign(nc * 4, 0);
   M.plen.assign(nc * 3, 0);
   M.muscl_slot.assign(nc * 4, 0);
-  for (int64_t c = 0; c < nc; ++c) {
+  parallel_for(nc, [&](int64_t c0, int64_t c1) {
+  for (int64_t c = c0; c < c1; ++c) {
     const double* x0 = &X[tris[c * 3] * 3];
     const double* x1 = &X[tris[c * 3 + 1] * 3];
     const double* x2 = &X[tris[c * 3 + 2] * 3];
@@ -258,6 +291,7 @@ bool build_ref_mesh_2d(const double* X, int64_t nv, const int64_t* blines, const
         M.rvec[c * 12 + m * 3 + d] = M.center[f * 3 + d] - M.centroid[c * 3 + d];
     }
   }
+  });
   cell_links(M, 3, muscl_exact);
   return true;
 }
@@ -386,7 +420,8 @@ bool build_ref_mesh(const double* X, int64_t nv, const int64_t* btris, const int
   M.weight.assign(nc * 4, 0);
   M.plen.assign(nc * 3, 0);
   M.muscl_slot.assign(nc * 4, 0);
-  for (int64_t c = 0; c < nc; ++c) {
+  parallel_for(nc, [&](int64_t c0, int64_t c1) {
+  for (int64_t c = c0; c < c1; ++c) {
     const int64_t* p = &tets[c * 4];
     for (int d = 0; d < 3; ++d)
       M.centroid[c * 3 + d] =
@@ -414,6 +449,7 @@ bool build_ref_mesh(const double* X, int64_t nv, const int64_t* btris, const int
         M.rvec[c * 12 + m * 3 + d] = M.center[f * 3 + d] - M.centroid[c * 3 + d];
     }
   }
+  });
   cell_links(M, 4, muscl_exact);
   return true;
 }
@@ -535,9 +571,20 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
       }
     std::vector<int64_t> rank_ref(nc);
     for (int64_t p = 0; p < nc; ++p) rank_ref[S.cell_new2ref[p]] = p;
-    std::stable_sort(S.cell_new2ref.begin(), S.cell_new2ref.end(), [&](int64_t a, int64_t b) {
-      return col[a] != col[b] ? col[a] < col[b] : lowmask[a] < lowmask[b];
-    });
+    {
+      // stable counting sort by (colour, lower-neighbour pattern), RCM order inside a group
+      int32_t maxcol = 0;
+      for (int64_t c = 0; c < nc; ++c) maxcol = std::max(maxcol, col[c]);
+      std::vector<int64_t> start((size_t)(maxcol + 1) * 16 + 1, 0);
+      for (int64_t c = 0; c < nc; ++c) ++start[(size_t)col[c] * 16 + lowmask[c] + 1];
+      for (size_t k = 1; k < start.size(); ++k) start[k] += start[k - 1];
+      std::vector<int64_t> sorted(nc);
+      for (int64_t p = 0; p < nc; ++p) {
+        const int64_t c = S.cell_new2ref[p];
+        sorted[start[(size_t)col[c] * 16 + lowmask[c]]++] = c;
+      }
+      S.cell_new2ref.swap(sorted);
+    }
     S.rcm_rank.resize(nc);
     for (int64_t i = 0; i < nc; ++i) S.rcm_rank[i] = rank_ref[S.cell_new2ref[i]];
     S.cell_color.resize(nc);
@@ -560,17 +607,29 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
     else
       ff.push_back(f);
   }
-  auto by_owner = [&](int64_t a, int64_t b) {
-    const int64_t oa = S.cell_ref2new[M.owner[a]], ob = S.cell_ref2new[M.owner[b]];
-    if (oa != ob) return oa < ob;
-    const int64_t na = M.neigh[a] >= 0 ? S.cell_ref2new[M.neigh[a]] : -1;
-    const int64_t nb_ = M.neigh[b] >= 0 ? S.cell_ref2new[M.neigh[b]] : -1;
-    if (na != nb_) return na < nb_;
-    return a < b;
+  // order by (new owner, new neighbour or -1, reference id): the keys are computed once, so
+  // the sort compares integers instead of looking the renumbering up per comparison
+  auto sort_by_owner = [&](std::vector<int64_t>& ids) {
+    struct Key {
+      int64_t owner, neigh, id;
+    };
+    std::vector<Key> keys(ids.size());
+    parallel_for((int64_t)ids.size(), [&](int64_t q0, int64_t q1) {
+      for (int64_t q = q0; q < q1; ++q) {
+        const int64_t f = ids[q];
+        keys[q] = {S.cell_ref2new[M.owner[f]], M.neigh[f] >= 0 ? S.cell_ref2new[M.neigh[f]] : -1, f};
+      }
+    });
+    std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
+      if (a.owner != b.owner) return a.owner < b.owner;
+      if (a.neigh != b.neigh) return a.neigh < b.neigh;
+      return a.id < b.id;
+    });
+    for (size_t q = 0; q < ids.size(); ++q) ids[q] = keys[q].id;
   };
-  std::sort(fi.begin(), fi.end(), by_owner);
-  std::sort(fs.begin(), fs.end(), by_owner);
-  std::sort(ff.begin(), ff.end(), by_owner);
+  sort_by_owner(fi);
+  sort_by_owner(fs);
+  sort_by_owner(ff);
   S.nf_int = (int32_t)fi.size();
   S.nf_slip = (int32_t)fs.size();
   S.nf_free = (int32_t)ff.size();
@@ -624,7 +683,8 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
   S.w.resize(4 * nc);
   S.r.resize(12 * nc);
   S.cflags.assign(nc, 0);
-  for (int64_t i = 0; i < nc; ++i) {
+  parallel_for(nc, [&](int64_t i0, int64_t i1) {
+  for (int64_t i = i0; i < i1; ++i) {
     const int64_t c = S.cell_new2ref[i];
     S.vol[i] = M.vol[c];
     S.inv_vol[i] = 1.0 / M.vol[c];
@@ -670,6 +730,7 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
       S.gface[m * nc + i] = (M.owner[fo] == c) ? fnew : ~fnew;
     }
   }
+  });
   for (int32_t k = 0; k < S.n_extra; ++k) S.cflags[S.extra_cell[k]] |= 0x10;
 
   // ---- face arrays
@@ -679,7 +740,8 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
   S.fsrc_nb.resize(nf);
   S.fn.resize(3 * nf);
   S.farea.resize(nf);
-  for (int64_t j = 0; j < nf; ++j) {
+  parallel_for(nf, [&](int64_t j0, int64_t j1) {
+  for (int64_t j = j0; j < j1; ++j) {
     const int64_t f = S.face_new2ref[j];
     const int64_t o = M.owner[f], n = M.neigh[f];
     const int64_t on = S.cell_ref2new[o];
@@ -695,17 +757,20 @@ void build_soa(const RefMesh& M, double venkat_k, bool muscl_exact, bool renumbe
     for (int d = 0; d < 3; ++d) S.fn[d * nf + j] = M.nhat[f * 3 + d];
     S.farea[j] = M.area[f];
   }
+  });
 
   // ---- ELL slots of each face in its two cells
   S.f_m_own.assign(nf, -1);
   S.f_m_nb.assign(nf, -1);
-  for (int64_t j = 0; j < nf; ++j) {
-    const int32_t o = S.fown[j], n = S.fnb[j];
-    for (int m = 0; m < 4; ++m) {
-      if (S.cface[m * nc + o] == j) S.f_m_own[j] = (int8_t)m;
-      if (n >= 0 && S.cface[m * nc + n] == j) S.f_m_nb[j] = (int8_t)m;
+  parallel_for(nf, [&](int64_t j0, int64_t j1) {
+    for (int64_t j = j0; j < j1; ++j) {
+      const int32_t o = S.fown[j], n = S.fnb[j];
+      for (int m = 0; m < 4; ++m) {
+        if (S.cface[m * nc + o] == j) S.f_m_own[j] = (int8_t)m;
+        if (n >= 0 && S.cface[m * nc + n] == j) S.f_m_nb[j] = (int8_t)m;
+      }
     }
-  }
+  });
   // ---- colouring of the cell graph (no two adjacent cells share a colour): the balanced
   // colouring of the renumbering, or first fit in the given order without renumbering
   int32_t ncol = 0;
