@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <numeric>
@@ -29,15 +30,26 @@ namespace {
 
 const int kTetFace[4][3] = {{0, 2, 1}, {1, 2, 3}, {0, 3, 2}, {0, 1, 3}};
 
-// body(begin, end) over [0, n) in contiguous chunks on up to 16 threads.  Every index is
-// handled by exactly one call, so a loop whose iterations write disjoint elements and read
-// only what earlier loops wrote gives the serial loop's result.  A chunk whose thread cannot
-// be started runs on the calling thread.
+// Threads of the host mesh build: the BES_HOST_THREADS environment variable if set (>= 1),
+// else the hardware's, at most 16.
+int64_t host_threads() {
+  static const int64_t n = [] {
+    const char* e = std::getenv("BES_HOST_THREADS");
+    const int64_t want = e ? std::atoll(e) : 0;
+    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+    return std::min<int64_t>(want >= 1 ? want : hw, 16);
+  }();
+  return n;
+}
+
+// body(begin, end) over [0, n) in contiguous chunks on up to host_threads() threads.  Every
+// index is handled by exactly one call, so a loop whose iterations write disjoint elements and
+// read only what earlier loops wrote gives the serial loop's result.  A chunk whose thread
+// cannot be started runs on the calling thread.
 template <class F>
 void parallel_for(int64_t n, F&& body) {
   const int64_t kMinChunk = 1 << 15;
-  const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
-  const int64_t nt = std::min<int64_t>({hw, 16, (n + kMinChunk - 1) / kMinChunk});
+  const int64_t nt = std::min<int64_t>(host_threads(), (n + kMinChunk - 1) / kMinChunk);
   if (nt <= 1) {
     if (n > 0) body((int64_t)0, n);
     return;

@@ -234,3 +234,23 @@ def test_besi_parser_is_strict(line):
         with pytest.raises(lib.BesError) as e:
             lib.options_from_besi(p)
     assert e.value.code == 5
+
+
+def test_host_build_is_independent_of_the_thread_count():
+    """The host mesh build runs its independent per-cell and per-face loops on several threads;
+    one thread gives the same geometry and numbering (BES_HOST_THREADS is read once per
+    process, so each count runs in a process of its own)."""
+    import json
+    import subprocess
+    import sys
+    code = ("import json, sys; sys.path.insert(0, %r); from bes_gb300 import lib, meshgen; "
+            "g = lib.host_geometry(meshgen.gaussian_box(40, 20, 40, 1.05)); "
+            "print(json.dumps({k: v.ravel().tolist()[::97] for k, v in g.items()}))"
+            % os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    outs = []
+    for n in ("1", "8"):
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                           env=dict(os.environ, BES_HOST_THREADS=n), timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(json.loads(r.stdout.strip().splitlines()[-1]))
+    assert outs[0] == outs[1]
