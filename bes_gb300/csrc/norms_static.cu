@@ -28,9 +28,32 @@ constexpr int kStaticNormMaxBlocks = (int)(kStaticNormMaxCells / kNormBlock);  /
 // on the GPU (two streams, or two host threads) share it and race.
 __device__ __align__(256) double g_norm_partials[10 * kStaticNormMaxBlocks];
 
-constexpr int kMaxDevices = 64;
-double* g_partials_ptr[kMaxDevices] = {};
+// Device address of g_norm_partials per CUDA context.  The address is a property of the
+// context the module is loaded into, not of the device number: a caller that makes its own
+// (non-primary) context with the driver API gets the copy of the array in that context.
+constexpr int kMaxContexts = 64;
+struct ScratchAddress {
+  void* context;
+  double* partials;
+};
+ScratchAddress g_scratch[kMaxContexts] = {};
+int g_n_scratch = 0;
 std::mutex g_setup_mutex;
+
+// cuCtxGetCurrent through the runtime's driver entry point (the library links only cudart).
+typedef int (*CtxGetCurrentFn)(void**);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
 
 __device__ __forceinline__ double wsum(double x) {
 #pragma unroll
@@ -119,16 +142,27 @@ extern "C" int bes_residual_norms_static(const double* residual, int64_t n_cells
     return BES_ERR_INVALID;
   }
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+  if (cudaGetDevice(&dev) != cudaSuccess) {
     put_err(err, err_cap, "no usable current CUDA device");
+    return BES_ERR_CUDA;
+  }
+  CtxGetCurrentFn get_ctx = ctx_get_current();
+  if (!get_ctx) {
+    put_err(err, err_cap, "cuCtxGetCurrent is not available from the CUDA driver");
     return BES_ERR_CUDA;
   }
   double* partials = nullptr;
   {
-    // First call on a device: look up the device address of the scratch array once, with
-    // that device current.  (The host-side name g_norm_partials is not a device address.)
+    // First call in a CUDA context: look up the device address of the scratch array once,
+    // with that context current.  (The host-side name g_norm_partials is not a device
+    // address.)  With no context current yet, the lookup itself makes the device's primary
+    // context current, and the address is recorded under that context.
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_partials_ptr[dev]) {
+    void* cur = nullptr;
+    if (get_ctx(&cur) != 0) cur = nullptr;
+    for (int k = 0; cur && k < g_n_scratch; ++k)
+      if (g_scratch[k].context == cur) partials = g_scratch[k].partials;
+    if (!partials) {
       void* p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, g_norm_partials);
       if (e != cudaSuccess || !p) {
@@ -137,9 +171,17 @@ extern "C" int bes_residual_norms_static(const double* residual, int64_t n_cells
         put_err(err, err_cap, buf);
         return BES_ERR_CUDA;
       }
-      g_partials_ptr[dev] = static_cast<double*>(p);
+      if (!cur && (get_ctx(&cur) != 0 || !cur)) {
+        put_err(err, err_cap, "no current CUDA context after the scratch lookup");
+        return BES_ERR_CUDA;
+      }
+      if (g_n_scratch >= kMaxContexts) {
+        put_err(err, err_cap, "too many CUDA contexts have used this entry point (at most 64)");
+        return BES_ERR_CUDA;
+      }
+      g_scratch[g_n_scratch++] = {cur, static_cast<double*>(p)};
+      partials = static_cast<double*>(p);
     }
-    partials = g_partials_ptr[dev];
   }
   const int nblocks = (int)((n_cells + kNormBlock - 1) / kNormBlock);
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -195,9 +195,11 @@ int bes_last_kernel_times(bes_ctx* ctx, double* ms_out);
  * norms [10] (device memory: L2[5], then max[5]), with the block reduction of the explicit
  * iteration.  Its scratch is a fixed 1.25 MiB array in device memory owned by the library
  * (held on every GPU that loads the library until the process exits), so n_cells is limited to
- * 4,194,304; larger sizes return BES_ERR_INVALID with a message in err.  The first call on
- * each device looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  The scratch is shared by all calls:
+ * 4,194,304; larger sizes return BES_ERR_INVALID with a message in err.  The first call in
+ * each CUDA context (the device's primary context, or a context the caller made current with
+ * the driver API) looks up the array's device address in that context (cudaGetSymbolAddress)
+ * and keeps it for the process; make that first call before any stream capture, and do not
+ * call this entry point again after resetting the device.  The scratch is shared by all calls:
  * calls that overlap on the GPU race.  Returns after enqueueing (does not synchronise). */
 int bes_residual_norms_static(const double* residual, int64_t n_cells, double* norms,
                               void* stream, char* err, size_t err_cap);

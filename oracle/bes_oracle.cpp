@@ -1,5 +1,5 @@
 // CPU restatement of joel-ho/BES's steady residual/update path, with a C ABI for the tests.
-// TEST INFRASTRUCTURE ONLY (see bes_oracle.hpp).  Build: oracle/build_oracle.py.
+// TEST INFRASTRUCTURE ONLY (see bes_oracle.hpp).  Built by oracle/pyoracle.py build().
 #include "bes_oracle.hpp"
 
 #include <algorithm>

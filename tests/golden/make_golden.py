@@ -5,7 +5,9 @@ oracle/_ref/) on small generated meshes at OMP_NUM_THREADS=1 and stores its FP64
 as compressed .npz fixtures.  Only this script reads the reference; the fixtures are what
 the tests use (the reference is not available where the GPU tests run).
 
-    python tests/golden/make_golden.py [--ref /path/to/reference]
+    python tests/golden/make_golden.py --ref /path/to/reference
+
+The reference checkout may also be given as the environment variable BES_REFERENCE_DIR.
 """
 from __future__ import annotations
 
@@ -218,9 +220,11 @@ def run_kat(name, mach, n=96, seed=7):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("BES_REFERENCE_DIR"))
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
+    if not a.ref:
+        sys.exit("give the reference checkout with --ref or BES_REFERENCE_DIR")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={a.ref}", "-j8"],
                    check=True, stdout=subprocess.DEVNULL)
     if not os.path.exists(HARNESS):

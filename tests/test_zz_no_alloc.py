@@ -54,3 +54,19 @@ def test_static_norms_reject_oversized_input():
         lib.residual_norms_static(buf.data_ptr(), 4194305, buf.data_ptr(), 0)
     assert e.value.code == 1
     assert "4194304" in str(e.value)
+
+
+@pytest.mark.parametrize("n_cells", [1000, 4194304])
+def test_static_norms_match_numpy_at_odd_and_largest_sizes(n_cells):
+    # 1000 cells is not a multiple of the 256-cell reduction block; 4,194,304 cells fill the
+    # whole scratch array (16,384 blocks of partial sums).  Two calls in a row with different
+    # data: the second must not see the first one's partials.
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(n_cells)
+    for scale in (1.0, 1e-3):
+        R = rng.standard_normal((n_cells, 5)) * scale
+        got = _norms_static(torch, R)
+        l2 = np.sqrt((R * R).sum(axis=0))
+        mx = np.abs(R).max(axis=0)
+        want = np.concatenate([l2, mx])
+        assert np.all(np.abs(got - want) <= 1e-12 * want), (got, want)
