@@ -284,7 +284,6 @@ int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_co
   BES_CUDA_TRY(c, cudaMemcpy(c->pinf0_dev, c->pinf0_host.data(), 6 * nb * sizeof(double),
                              cudaMemcpyHostToDevice));
   c->active_host.assign(nb, 1);
-  if (nb > 1) c->cond_imp.assign(nb, bes_ctx::CondImplicit());
   BES_CUDA_TRY(c, cudaMemcpy(c->active_dev, c->active_host.data(), nb * sizeof(int32_t),
                              cudaMemcpyHostToDevice));
   c->prm.pinf_dev = c->pinf_dev;
@@ -316,10 +315,7 @@ void bes_destroy(bes_ctx* ctx) {
   for (int k = 0; k < 8; ++k)
     for (int q = 0; q < 6; ++q)
       if (ctx->kev[k][q]) cudaEventDestroy(ctx->kev[k][q]);
-  if (ctx->imp.factor_graph) cudaGraphExecDestroy(ctx->imp.factor_graph);
-  if (ctx->imp.apply_graph) cudaGraphExecDestroy(ctx->imp.apply_graph);
-  for (cudaGraphExec_t g : ctx->imp.colour_graphs) cudaGraphExecDestroy(g);
-  for (cudaEvent_t e : ctx->prof.pool) cudaEventDestroy(e);
+  implicit_release(ctx);
   for (void* p : ctx->allocations) cudaFree(p);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -338,13 +334,7 @@ int bes_set_freestream_state(bes_ctx* ctx) {
   if (!ctx) return BES_ERR_INVALID;
   // A new solve: step counter, CFL control and freestream ramp restart at step 0.
   ctx->host_step = 0;
-  ctx->imp.step_count = 0;
-  ctx->imp.cfl_actual = ctx->opt.courant_num;
-  for (int v = 0; v < 5; ++v) ctx->imp.maxres[v] = ctx->imp.maxres_old[v] = 0.0;
-  for (auto& ci : ctx->cond_imp) {
-    ci = bes_ctx::CondImplicit();
-    ci.cfl_actual = ctx->opt.courant_num;
-  }
+  implicit_reset(ctx);
   const int64_t zero = 0;
   BES_CUDA_TRY(ctx, cudaMemcpy(ctx->step_dev, &zero, sizeof(zero), cudaMemcpyHostToDevice));
   // GasPerfect_::computeAllConservedVariable of the step-0 freestream primitives
@@ -590,6 +580,55 @@ int bes_set_active(bes_ctx* ctx, const int32_t* active) {
                                     ctx->nb * sizeof(int32_t), cudaMemcpyHostToDevice,
                                     ctx->stream));
   BES_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BES_OK;
+}
+
+int bes_set_condition(bes_ctx* ctx, int32_t cond, const double* mach, const double* U) {
+  if (!ctx || cond < 0 || cond >= ctx->nb) return BES_ERR_INVALID;
+  const int64_t nc = ctx->soa.nc;
+  double* p = &ctx->pinf0_host[6 * cond];
+  if (mach) {
+    p[0] = 1.0;
+    for (int d = 0; d < 3; ++d) p[1 + d] = d < ctx->ref.dim ? mach[d] : 0.0;
+    p[4] = 1.0 / ctx->opt.specific_heat_ratio;
+    p[5] = 1.0 / (ctx->opt.specific_heat_ratio * ctx->opt.gas_constant);
+    if (cond == 0)
+      for (int i = 0; i < 6; ++i) ctx->prm.pinf[i] = p[i];
+    BES_CUDA_TRY(ctx, cudaMemcpy(ctx->pinf0_dev + 6 * cond, p, 6 * sizeof(double),
+                                 cudaMemcpyHostToDevice));
+  }
+  // the condition's state in reference numbering, or its step-0 freestream
+  std::vector<double> Uh(5 * nc);
+  if (U) {
+    std::copy(U, U + 5 * nc, Uh.begin());
+  } else {
+    double q[6];
+    freestream_from(p, ctx->prm.ramp_steps, ctx->prm.ramp_frac, 0, q);
+    double Uf[5];
+    Uf[0] = q[0];
+    double k2 = 0;
+    for (int d = 0; d < 3; ++d) {
+      Uf[1 + d] = Uf[0] * q[1 + d];
+      k2 += q[1 + d] * q[1 + d];
+    }
+    Uf[4] = Uf[0] * (ctx->prm.gas.cv * q[5] + k2 / 2.0);
+    for (int64_t i = 0; i < nc; ++i)
+      for (int v = 0; v < 5; ++v) Uh[i * 5 + v] = Uf[v];
+  }
+  BES_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->stage, Uh.data(), 5 * nc * sizeof(double),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+  state_from_stage_kernel<<<1024, 256, 0, ctx->stream>>>(
+      (int)nc, 1, ctx->new2ref_dev, ctx->stage, ctx->U[ctx->cur] + (int64_t)cond * 5 * nc);
+  ++ctx->launches;
+  if (cond < (int)ctx->imp.ctl.size()) {
+    ctx->imp.ctl[cond] = SlotCtl();
+    ctx->imp.ctl[cond].cfl_actual = ctx->opt.courant_num;
+  }
+  ctx->active_host[cond] = 1;
+  BES_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->active_dev, ctx->active_host.data(),
+                                    ctx->nb * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+  BES_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  BES_CUDA_TRY(ctx, cudaGetLastError());
   return BES_OK;
 }
 

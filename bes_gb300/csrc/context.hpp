@@ -63,21 +63,78 @@ struct ExplicitGraph {
 }  // namespace bes
 
 namespace bes {
-// Device buffers of the implicit path (allocated when the context is created for it).
+// Device-side state of restarted GMRES for every condition ("slot") of a context.  Each array
+// holds one entry (or one fixed-size block) per slot; the Arnoldi loop, the Givens rotations,
+// the restart decision and the convergence test run on the device (krylov_kernels.cuh).
+constexpr int kMaxRestart = 32;      // GMRES_RESTART limit (Hessenberg columns)
+constexpr int kHld = kMaxRestart;    // row stride of the Hessenberg matrix
+constexpr int kGsLd = 128;           // Gram-Schmidt scalars per slot (see krylov_kernels.cuh)
+struct GmresDev {
+  double* H = nullptr;    // [slot][(kMaxRestart + 1) * kHld] rotated Hessenberg matrix
+  double* cs = nullptr;   // [slot][kMaxRestart] Givens cosines
+  double* sn = nullptr;   // [slot][kMaxRestart] Givens sines
+  double* g = nullptr;    // [slot][kMaxRestart + 1] rotated right-hand side
+  double* y = nullptr;    // [slot][kMaxRestart] least-squares solution of the cycle
+  double* sc = nullptr;   // [slot][8] norm_b, eps, beta, 1/beta, |r|, rel
+  int32_t* lin = nullptr;     // [slot] 1 while the slot's linear solve runs
+  int32_t* cyc = nullptr;     // [slot] 1 while the slot's current restart cycle runs
+  int32_t* jc = nullptr;      // [slot] Arnoldi steps done in the current cycle
+  int32_t* iter = nullptr;    // [slot] Arnoldi steps done in this solve
+  int32_t* second = nullptr;  // [slot] Arnoldi steps that needed a second Gram-Schmidt pass
+  int32_t* status = nullptr;  // [slot] BES_OK, or BES_ERR_TIMEOUT when the cycle guard stopped it
+  int32_t* cycles = nullptr;  // [slot] restart cycles of this solve
+  double* dev = nullptr;      // [slot][kGsLd] Gram-Schmidt scalars (FP64)
+  float* devf = nullptr;      // [slot][kGsLd] their FP32 copies
+  unsigned long long* counters = nullptr;  // [2] Arnoldi and restart-cycle bodies executed
+};
+
+// What one implicit step reports per slot (read back once per step).
+struct StepResult {
+  double norms[15];  // L2[5], max[5] of the Dt/V-scaled right-hand side, L2[5] of R
+  double rel;        // final relative linear residual
+  int32_t iters;     // linear iterations
+  int32_t second;    // of which needed a second Gram-Schmidt pass
+  int32_t status;    // BES_OK or BES_ERR_TIMEOUT
+  int32_t active;    // 1 if the slot took the step
+};
+
+// Host-side controller of one condition's implicit solve (CFL control, step counters).
+struct SlotCtl {
+  double cfl_actual = 0;
+  double maxres[5] = {0, 0, 0, 0, 0};
+  double maxres_old[5] = {0, 0, 0, 0, 0};
+  int64_t step_count = 0;
+  int64_t host_step = 0;
+};
+
+// Device buffers of the implicit path (allocated when the context is created for it).  Every
+// condition of a batched context is a slot: the Krylov side (matrix copies the solver reads,
+// basis, vectors, GMRES state) is per slot and the solver advances all slots together.  The
+// FP32 assembly and factorisation scratch of the 16-bit storage (precision 2) is shared: the
+// slots are assembled and factored one after another into it and packed into their own
+// 16-bit copies.
 struct ImplicitBuffers {
   int prec = 0;          // 0: FP64 system, 1: FP32 system (defect correction; precision 1 or 2)
   size_t tsize = 8;      // sizeof(T)
-  void* A = nullptr;     // ELL blocks [5 slots][25][nc]
+  int nslot = 1;
+  int64_t ldv = 0;       // Krylov vector stride: 5 nc rounded up to 64 elements
+  // system in T: ELL blocks [5 slots][25][nc]; per condition (precision 0/1) or one shared
+  // scratch (precision 2); sA etc. are the per-condition strides in elements (0: shared)
+  void* A = nullptr;
   void* LU = nullptr;    // block-ILU(0) factors in the same layout (ILU only)
   void* Dinv = nullptr;  // [25][nc] inverse diagonal (Jacobi) / inverse U_ii (ILU)
-  void* Dc = nullptr;    // per-face diagonal contributions [2][25][nf]
-  void* b = nullptr;     // right-hand side in T [5][nc]
-  void* V = nullptr;     // Krylov basis [(m+1)][5 nc]
-  void* Z = nullptr;     // [5 nc]
-  void* W = nullptr;     // [5 nc]
-  void* X = nullptr;     // solution dW [5 nc]
+  int64_t sA = 0, sDinv = 0;
+  void* Dc = nullptr;    // per-face diagonal contributions [2][25][nf] (shared)
+  // Krylov side, per condition
+  void* b = nullptr;     // right-hand side in T [ldv]
+  void* V = nullptr;     // Krylov basis [(m+1)][ldv] (FP16 with precision 2)
+  int64_t sV = 0;        // basis elements per condition
+  void* Z = nullptr;     // [ldv]
+  void* W = nullptr;     // [ldv]
+  void* X = nullptr;     // solution dW [ldv]
   // precision 2: 16-bit block-scaled copies (half2 [slot][13][nc] + FP32 scale [slot][nc]) of
-  // A (5 slots), the off-diagonal ILU factors (4 slots) and the inverse diagonal (1 slot)
+  // A (5 slots), the off-diagonal ILU factors (4 slots) and the inverse diagonal (1 slot), per
+  // condition
   bool packed = false;
   void* A16 = nullptr;
   float* As = nullptr;
@@ -89,40 +146,48 @@ struct ImplicitBuffers {
   // newest vector, the preconditioner's input
   bool basis16 = false;
   void* Vx = nullptr;
-  double* rhs = nullptr;       // FP64 right-hand side [5][nc]
-  double* red = nullptr;       // reduction partials [64][kRedBlocks]
-  double* red_out = nullptr;   // reduced values [128]
-  float* red_out_f = nullptr;  // FP32 copies of Gram-Schmidt coefficients [128]
-  double* coef = nullptr;      // small coefficient vectors [64]
+  double* rhs = nullptr;       // FP64 right-hand side [slot][5][nc]
+  double* red = nullptr;       // reduction partials [slot][64][red_ld]
+  int64_t red_ld = 0;
+  GmresDev gm;
+  StepResult* res = nullptr;   // [slot]
+  std::vector<StepResult> res_host;
+  double* cfl_dev = nullptr;   // [slot] CFL of the current step
+  int32_t* act = nullptr;      // [slot] slots that take the current step
+  int32_t* guard_dev = nullptr;  // restart-cycle limit of a linear solve (device copy)
+  int32_t guard = 0;             // 0: linear_solver_max_iter + 1 cycles
   int8_t* m_own = nullptr;     // per face local index in owner / neighbour
   int8_t* m_nb = nullptr;
   int32_t* stage_rows = nullptr;  // block-ILU(0) rows grouped by stage
   int32_t* ilu_pos = nullptr;     // factorisation position of each cell
-  cudaGraphExec_t factor_graph = nullptr;  // ILU factorisation, all stages
-  cudaGraphExec_t apply_graph = nullptr;   // ILU forward+backward sweep, in place on Z
   bool use_colour_ranges = false;          // colour order on contiguous colour ranges
-  std::vector<cudaGraphExec_t> colour_graphs;  // sweeps from V_0..V_m, then from W, into Z
-  double cfl_actual = 0;
-  double maxres[5] = {0, 0, 0, 0, 0};
-  double maxres_old[5] = {0, 0, 0, 0, 0};
-  int64_t step_count = 0;
-  int last_iters = 0;
+  // one graph per implicit step: [profiled][snapshot], built on first use; kernel nodes of its
+  // sections (top level, one slot's assembly, one Arnoldi step, one restart-cycle end)
+  cudaGraphExec_t step_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  int64_t nodes_top[2] = {0, 0}, nodes_slot[2] = {0, 0}, nodes_arn[2] = {0, 0},
+          nodes_loop[2] = {0, 0};
+  cudaStream_t cap[2] = {nullptr, nullptr};  // streams capturing conditional bodies
+  unsigned long long counters_host[2] = {0, 0};
+  std::vector<SlotCtl> ctl;    // [slot]
+  int64_t step_count = 0;      // step calls of the context
   int64_t total_lin_iters = 0;
   int64_t gs_second_passes = 0;  // Arnoldi steps that needed a second Gram-Schmidt pass
+  int64_t host_syncs = 0;        // host synchronisations inside bes_implicit_steps
+  int last_iters = 0;
   double last_err = 0;
 };
 }  // namespace bes
 
 namespace bes {
-// Optional event timing of the implicit path by kernel category (bes_profile).
+// Optional timing of the implicit path by kernel category (bes_profile): one-thread kernels
+// read the GPU's global nanosecond timer before and after every category's work inside the
+// step graph (events cannot be recorded inside its conditional nodes) and accumulate the
+// elapsed time per category on the device.
 enum ProfCat { PROF_RESIDUAL = 0, PROF_JACOBIAN, PROF_ASSEMBLE, PROF_ILU_FACTOR, PROF_PRECOND,
                PROF_SPMV, PROF_ORTHO, PROF_OTHER, PROF_NCAT };
 struct Profiler {
   bool on = false;
-  std::vector<cudaEvent_t> pool;                     // pairs: begin at 2k, end at 2k+1
-  int next = 0;                                      // next free pair
-  std::vector<std::pair<int, int>> pending;          // (category, pair)
-  int open_pair[PROF_NCAT];
+  unsigned long long* dev = nullptr;  // [2 * PROF_NCAT + PROF_NCAT]: open stamp, ns, count
   double ms[PROF_NCAT] = {};
   int64_t count[PROF_NCAT] = {};
 };
@@ -166,16 +231,6 @@ struct bes_ctx {
   int32_t* active_dev = nullptr;     // [nb]
   std::vector<double> pinf0_host;    // [nb][6]
   std::vector<int32_t> active_host;  // [nb]
-  // implicit batches step the conditions one after another through one set of implicit
-  // buffers; each condition keeps its own CFL controller and step counters
-  struct CondImplicit {
-    double cfl_actual = 0;
-    double maxres[5] = {0, 0, 0, 0, 0};
-    double maxres_old[5] = {0, 0, 0, 0, 0};
-    int64_t step_count = 0;
-    int64_t host_step = 0;
-  };
-  std::vector<CondImplicit> cond_imp;  // [nb] when nb > 1
   // state exchange with the caller: raw copies of [nb][nc][5] (reference numbering) into a
   // staging array, permuted and transposed on the device
   double* stage = nullptr;             // [nb][nc][5]
@@ -202,7 +257,6 @@ int implicit_allocate(bes_ctx* ctx);  // buffers of the implicit path
 }  // namespace bes
 
 namespace bes {
-void prof_begin(bes_ctx* c, int cat);
-void prof_end(bes_ctx* c, int cat);
-void prof_collect(bes_ctx* c);  // after a synchronisation: accumulate finished pairs
+void implicit_reset(bes_ctx* c);  // a new solve: CFL control and step counters of every slot
+void implicit_release(bes_ctx* c);  // graphs of the implicit path
 }  // namespace bes

@@ -38,12 +38,14 @@ __device__ __forceinline__ bool condition_frozen(const Params& prm) {
   return prm.active != nullptr && prm.active[blockIdx.y] == 0;
 }
 
-// Cell sweep.  U is [5][nc]; RS is [5][ldr] with ldr >= nc*nslots + n_extra.
+// Cell sweep.  U is [5][nc]; RS is [5][ldr] with ldr >= nc*nslots + n_extra.  cfl_dev (may
+// be null): a per-condition CFL number that replaces cfl (the implicit step's CFL control).
 template <bool STAGE0, bool WRITE_GL>
 __global__ void __launch_bounds__(kBlock) cell_recon_kernel(
     DevMesh m, Params prm, const double* __restrict__ U, double* __restrict__ RS, int64_t ldr,
     double* __restrict__ dt, double cfl, int local_dt, unsigned long long* __restrict__ dtmin,
-    double* __restrict__ G_out, double* __restrict__ phi_out) {
+    double* __restrict__ G_out, double* __restrict__ phi_out,
+    const double* __restrict__ cfl_dev = nullptr) {
   const int nc = m.nc;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (condition_frozen(prm)) return;
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(kBlock) cell_recon_kernel(
       double spec = 0.0;
 #pragma unroll
       for (int d = 0; d < 3; ++d) spec += (cs + fabs(u[1 + d] * ir)) * m.plen[(int64_t)d * nc + c];
-      dt_c = cfl * m.vol[c] / spec;
+      dt_c = (cfl_dev ? cfl_dev[blockIdx.y] : cfl) * m.vol[c] / spec;
       dt[c] = dt_c;
     }
   }

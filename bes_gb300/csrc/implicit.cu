@@ -1,17 +1,27 @@
 // Implicit (backward-Euler) pseudo-time step on the GPU: SolverImplicit::timeStep_
 // (src/SolverImplicit.cpp:293-345) with the AMGCL solve (src/CoefficientMatrix.cpp:210-325)
-// replaced by right-preconditioned restarted GMRES with a block-Jacobi or colour-ordered
-// block-ILU(0) preconditioner.  The system (Jacobian, preconditioner, Krylov vectors) is FP64
-// for the plain method or FP32 for the defect correction; the residual, right-hand side,
-// update and norms are always FP64.
+// replaced by right-preconditioned restarted GMRES with a block-Jacobi or block-ILU(0)
+// preconditioner.  The system (Jacobian, preconditioner, Krylov vectors) is FP64 for the plain
+// method or FP32 for the defect correction; the residual, right-hand side, update and norms
+// are always FP64.
+//
+// Every condition of a context is a slot, and one implicit step of all slots is ONE CUDA graph
+// launch: the residual of every slot (one launch per kernel, slots on the grid's y axis), then
+// per slot the Jacobians, the assembly and the factorisation (inside an IF node that skips a
+// frozen slot), then the linear solves of all slots together: a WHILE node over restart
+// cycles whose body holds one IF node per Arnoldi step, the Arnoldi kernels batched over the
+// slots and the GMRES bookkeeping (Hessenberg column, Givens rotations, least squares,
+// restart and convergence) in small device kernels (krylov_kernels.cuh).  The host reads the
+// step's norms and linear-solve statistics back once per step and runs the CFL control.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <type_traits>
 #include <vector>
 
 #include "context.hpp"
-#include "implicit_kernels.cuh"
+#include "krylov_kernels.cuh"
 
 using namespace bes;
 
@@ -40,178 +50,663 @@ int imp_malloc(bes_ctx* c, void** p, size_t bytes) {
 
 inline int64_t basis_stride(int64_t nc) { return (5 * nc + 63) / 64 * 64; }
 
-template <class T>
+inline bool uses_ilu(const bes_ctx* c) { return c->opt.linear_solver == 1 || c->opt.linear_solver == 2; }
+
+// Device views of the implicit buffers: T is the system's type, B the basis element type.
+template <class T, class B>
 struct Sys {
   bes_ctx* c;
-  int nc;
-  int64_t N;
-  T* A;
-  T* LU;
-  T* Dinv;
-  T* Dc;
-  T* b;
-  T* V;
-  T* Z;
-  T* W;
-  T* X;
-  bool packed;  // precision 2: the Krylov products and sweeps read the 16-bit copies
-  const __half2 *A16, *LU16, *D16;
-  const float *As, *LUs, *Ds;
-  bool basis16;  // precision 2: FP16 Krylov basis; the preconditioner reads Vx
-  T* Vx;         // FP32 copy of the newest basis vector (basis16 only)
-  cudaStream_t s;
+  int nc, nslot;
+  int64_t N, ldv, sV, sA, sDinv;
+  T *A, *LU, *Dinv, *Dc, *b, *Z, *W, *X, *Vx;
+  B* V;
+  bool packed, basis16;
+  __half2 *A16, *LU16, *D16;
+  float *As, *LUs, *Ds;
+  cudaStream_t s;  // the stream being captured (switched inside conditional bodies)
+  dim3 vgrid;      // vector kernels: kRedBlocks blocks per slot
+  int nthr;        // control kernels: one thread per slot, rounded up to a warp
   explicit Sys(bes_ctx* ctx) : c(ctx) {
     ImplicitBuffers& I = ctx->imp;
     nc = ctx->soa.nc;
+    nslot = I.nslot;
     N = 5LL * nc;
-    ldv = basis_stride(nc);
+    ldv = I.ldv;
+    sV = I.sV;
+    sA = I.sA;
+    sDinv = I.sDinv;
     A = (T*)I.A;
     LU = (T*)I.LU;
     Dinv = (T*)I.Dinv;
     Dc = (T*)I.Dc;
     b = (T*)I.b;
-    V = (T*)I.V;
     Z = (T*)I.Z;
     W = (T*)I.W;
     X = (T*)I.X;
+    Vx = (T*)I.Vx;
+    V = (B*)I.V;
     packed = I.packed;
-    A16 = (const __half2*)I.A16;
-    LU16 = (const __half2*)I.LU16;
-    D16 = (const __half2*)I.D16;
+    basis16 = I.basis16;
+    A16 = (__half2*)I.A16;
+    LU16 = (__half2*)I.LU16;
+    D16 = (__half2*)I.D16;
     As = I.As;
     LUs = I.LUs;
     Ds = I.Ds;
-    basis16 = I.basis16;
-    Vx = (T*)I.Vx;
     s = ctx->stream;
+    vgrid = dim3(kRedBlocks, nslot);
+    nthr = std::min(kMaxSlots, (nslot + 31) / 32 * 32);
   }
-  int64_t ldv;  // stride of the Krylov basis: N rounded up to 64 elements (16-byte loads)
-  T* Vk(int k) const { return V + (int64_t)k * ldv; }
+  // per-slot views
+  SlotPtr<T> vec(T* p) const { return slots(p, ldv); }
+  SlotPtr<const T> cvec(const T* p) const { return cslots(p, ldv); }
+  SlotPtr<B> basis(int k) const { return slots(V + (int64_t)k * ldv, sV); }
+  SlotPtr<const B> cbasis(int k) const { return cslots(V + (int64_t)k * ldv, sV); }
+  SlotPtr<double> red() const { return slots(c->imp.red, 64 * c->imp.red_ld); }
+  SlotPtr<const double> cred() const { return cslots(c->imp.red, 64 * c->imp.red_ld); }
+  SlotPtr<double> dev(int off = 0) const { return slots(c->imp.gm.dev + off, (int64_t)kGsLd); }
+  SlotPtr<const double> cdev() const { return cslots(c->imp.gm.dev, (int64_t)kGsLd); }
+  SlotPtr<float> devf() const { return slots(c->imp.gm.devf, (int64_t)kGsLd); }
+  SlotPtr<const float> cdevf() const { return cslots(c->imp.gm.devf, (int64_t)kGsLd); }
+  // the preconditioner's input for Arnoldi step j: the basis vector, or its FP32 copy
+  SlotPtr<const T> precond_in(int j) const {
+    if constexpr (std::is_same<T, B>::value) return cslots((const T*)(V + (int64_t)j * ldv), sV);
+    else return cvec(Vx);
+  }
+  // system arrays of slot k (the shared scratch when sA == 0)
+  T* A_of(int k) const { return A + (int64_t)k * sA; }
+  T* LU_of(int k) const { return LU + (int64_t)k * sA; }
+  T* Dinv_of(int k) const { return Dinv + (int64_t)k * sDinv; }
 };
 
-// reduce rows of c->imp.red and copy them to the host
-int reduce_to_host(bes_ctx* c, int nrows, int nblocks, int nsum, int sqrt_sums, double* host) {
-  reduce_rows_kernel<<<nrows, 256, 0, c->stream>>>(c->imp.red, nblocks, nsum, sqrt_sums,
-                                                   c->imp.red_out);
-  ++c->launches;
-  IMP_TRY(c, cudaMemcpyAsync(host, c->imp.red_out, nrows * sizeof(double), cudaMemcpyDeviceToHost,
-                             c->stream));
-  IMP_TRY(c, cudaStreamSynchronize(c->stream));
+// Kernel nodes of a graph (not descending into conditional bodies).
+int64_t kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return 0;
+  int64_t k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+// Timing stamps around a kernel category, in the profiled variant of the step graph only.
+thread_local bool t_stamps = false;
+void stamp(bes_ctx* c, cudaStream_t s, int cat, int begin) {
+  if (!t_stamps) return;
+  prof_stamp_kernel<<<1, 1, 0, s>>>(c->prof.dev, cat, begin);
+}
+
+// Add a conditional node (IF or WHILE on handle h) after the current capture dependencies of
+// `parent` and start capturing its body on `child`.
+int begin_conditional(bes_ctx* c, cudaStream_t parent, cudaStream_t child,
+                      cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  IMP_TRY(c, cudaStreamGetCaptureInfo(parent, &st, nullptr, &g, &deps, nullptr, &nd));
+  if (st != cudaStreamCaptureStatusActive) {
+    c->last_error = "conditional node outside a capture";
+    return BES_ERR_CUDA;
+  }
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = type;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  IMP_TRY(c, cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+  IMP_TRY(c, cudaStreamUpdateCaptureDependencies(parent, &node, nullptr, 1,
+                                                 cudaStreamSetCaptureDependencies));
+  IMP_TRY(c, cudaStreamBeginCaptureToGraph(child, p.conditional.phGraph_out[0], nullptr, nullptr,
+                                           0, cudaStreamCaptureModeRelaxed));
   return BES_OK;
 }
 
-// 16-bit block-scaled copies (precision 2; T is float there)
-template <class T>
-void enqueue_pack(const Sys<T>& S, const T* src, int slot0, int nslots, void* H, float* sc) {
-  if constexpr (std::is_same<T, float>::value) {
-    pack_blocks_kernel<<<dim3(nblk(S.nc, 256), nslots), 256, 0, S.s>>>(src, slot0, S.nc,
-                                                                       (__half2*)H, sc);
-    ++S.c->launches;
+// End the body's capture; *kernels receives its kernel node count.
+int end_conditional(bes_ctx* c, cudaStream_t child, int64_t* kernels) {
+  cudaGraph_t body = nullptr;
+  IMP_TRY(c, cudaStreamEndCapture(child, &body));
+  *kernels = kernel_nodes(body);
+  return BES_OK;
+}
+
+// ---- Krylov side, batched over slots -----------------------------------------------------
+
+// Z = M^{-1} in for every slot whose run flag is set
+template <class T, class B>
+void enqueue_precond(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> in, const int32_t* run) {
+  bes_ctx* c = S.c;
+  const SoaMesh& M = c->soa;
+  const DevMesh& m = c->dm;
+  SlotPtr<T> Z = S.vec(S.Z);
+  if (!uses_ilu(c)) {
+    if constexpr (std::is_same<T, float>::value) {
+      if (S.packed) {
+        jacobi_apply_packed_kernel<<<dim3(nblk(S.nc, 256), S.nslot), 256, 0, s>>>(
+            S.nc, cslots((const __half2*)S.D16, 13LL * S.nc), cslots((const float*)S.Ds, (int64_t)S.nc),
+            in, Z, run);
+        return;
+      }
+    }
+    jacobi_apply_kernel<T><<<dim3(nblk(S.nc, 256), S.nslot), 256, 0, s>>>(
+        S.nc, cslots((const T*)S.Dinv, S.sDinv), in, Z, run);
+    return;
+  }
+  if (c->imp.use_colour_ranges) {
+    // colours 1..C-2 forward, the last colour's two solves fused, colours C-2..0 backward
+    const int C = M.n_stages;
+    const int s1 = M.stage_off[1];
+    auto launch = [&](int k, bool lower, bool upper) {
+      const int r0 = M.stage_off[k], r1 = M.stage_off[k + 1];
+      const dim3 grid(nblk(r1 - r0, 128), S.nslot);
+      if constexpr (std::is_same<T, float>::value) {
+        if (S.packed) {
+          auto H = cslots((const __half2*)S.LU16, 52LL * S.nc);
+          auto HS = cslots((const float*)S.LUs, 4LL * S.nc);
+          auto D = cslots((const __half2*)S.D16, 13LL * S.nc);
+          auto DS = cslots((const float*)S.Ds, (int64_t)S.nc);
+          if (lower && !upper)
+            ilu_colour_packed_kernel<true, false><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run);
+          else if (lower)
+            ilu_colour_packed_kernel<true, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run);
+          else
+            ilu_colour_packed_kernel<false, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run);
+          return;
+        }
+      }
+      auto L = cslots((const T*)S.LU, S.sA);
+      auto D = cslots((const T*)S.Dinv, S.sDinv);
+      if (lower && !upper)
+        ilu_colour_kernel<T, true, false><<<grid, 128, 0, s>>>(m, r0, r1, s1, L, D, in, Z, run);
+      else if (lower)
+        ilu_colour_kernel<T, true, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, L, D, in, Z, run);
+      else
+        ilu_colour_kernel<T, false, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, L, D, in, Z, run);
+    };
+    for (int k = 1; k < C - 1; ++k) launch(k, true, false);
+    launch(C - 1, true, true);
+    for (int k = C - 2; k >= 0; --k) launch(k, false, true);
+    return;
+  }
+  // level-scheduled stages (RCM order), in place on Z
+  copy_vec_kernel<T><<<S.vgrid, 256, 0, s>>>(Z, in, S.N, run);
+  auto L = cslots((const T*)S.LU, S.sA);
+  auto D = cslots((const T*)S.Dinv, S.sDinv);
+  for (int k = 0; k < M.n_stages; ++k) {
+    const int n = M.stage_off[k + 1] - M.stage_off[k];
+    ilu_lower_kernel<T><<<dim3(nblk(n, 128), S.nslot), 128, 0, s>>>(
+        m, c->imp.stage_rows + M.stage_off[k], n, c->imp.ilu_pos, L, Z, run);
+  }
+  for (int k = M.n_stages - 1; k >= 0; --k) {
+    const int n = M.stage_off[k + 1] - M.stage_off[k];
+    ilu_upper_kernel<T><<<dim3(nblk(n, 128), S.nslot), 128, 0, s>>>(
+        m, c->imp.stage_rows + M.stage_off[k], n, c->imp.ilu_pos, L, D, Z, run);
   }
 }
 
 // y = A x, or y = b - A x when b is given
-template <class T>
-void spmv(const Sys<T>& S, const T* x, const T* b, T* y) {
+template <class T, class B>
+void enqueue_spmv(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> x, SlotPtr<const T> b,
+                  SlotPtr<T> y, const int32_t* run) {
+  const dim3 grid(nblk(S.nc, 256), S.nslot);
   if constexpr (std::is_same<T, float>::value) {
     if (S.packed) {
-      spmv_packed_kernel<<<nblk(S.nc, 256), 256, 0, S.s>>>(S.c->dm, S.A16, S.As, x, b, y);
-      ++S.c->launches;
+      spmv_packed_kernel<<<grid, 256, 0, s>>>(S.c->dm, cslots((const __half2*)S.A16, 65LL * S.nc),
+                                              cslots((const float*)S.As, 5LL * S.nc), x, b, y, run);
       return;
     }
   }
-  spmv_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.c->dm, S.A, x, b, y);
-  ++S.c->launches;
+  spmv_kernel<T><<<grid, 256, 0, s>>>(S.c->dm, cslots((const T*)S.A, S.sA), x, b, y, run);
 }
 
-inline bool uses_ilu(const bes_ctx* c) { return c->opt.linear_solver == 1 || c->opt.linear_solver == 2; }
-
-// Enqueue the block-ILU(0) sweeps in place on S.Z (stage by stage), for graph capture.
-template <class T>
-void enqueue_ilu_sweeps(const Sys<T>& S) {
+// Body of the IF node of Arnoldi step j (slots with a running cycle): w = A M^{-1} v_j,
+// Gram-Schmidt against v_0..v_j, v_{j+1}, and the Givens update of the Hessenberg column.
+template <class T, class B>
+void enqueue_arnoldi(const Sys<T, B>& S, cudaStream_t s, int j, const GmresParam& P,
+                     const GmresHandles& h) {
   bes_ctx* c = S.c;
-  const SoaMesh& M = c->soa;
-  for (int k = 0; k < M.n_stages; ++k) {
-    const int n = M.stage_off[k + 1] - M.stage_off[k];
-    ilu_lower_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
-                                                       n, c->imp.ilu_pos, S.LU, S.Z, S.Z);
-  }
-  for (int k = M.n_stages - 1; k >= 0; --k) {
-    const int n = M.stage_off[k + 1] - M.stage_off[k];
-    ilu_upper_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
-                                                       n, c->imp.ilu_pos, S.LU, S.Dinv, S.Z);
-  }
+  const int32_t* cyc = c->imp.gm.cyc;
+  const int nv = j + 1;
+  stamp(c, s, PROF_PRECOND, 1);
+  enqueue_precond(S, s, S.precond_in(j), cyc);
+  stamp(c, s, PROF_PRECOND, 0);
+  stamp(c, s, PROF_SPMV, 1);
+  enqueue_spmv(S, s, S.cvec(S.Z), SlotPtr<const T>{nullptr, 0}, S.vec(S.W), cyc);
+  stamp(c, s, PROF_SPMV, 0);
+  stamp(c, s, PROF_ORTHO, 1);
+  const auto Vb = S.cbasis(0);
+  launch_gs_dots<T, B>(nv, S.vgrid, s, Vb, S.ldv, S.cvec(S.W), S.N, S.red(), cyc);
+  reduce_slots_kernel<<<dim3(nv + 1, S.nslot), 256, 0, s>>>(S.cred(), kRedBlocks, nv + 1, 0,
+                                                            S.dev(), cyc);
+  gs_decide_kernel<<<dim3(1, S.nslot), 64, 0, s>>>(S.dev(), S.devf(), nv, 1, cyc);
+  launch_gs_update<T, B, GS_FINAL1>(nv, S.vgrid, s, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
+                                    S.ldv, S.cdev(), S.cdevf(), S.N, S.red(), cyc);
+  launch_gs_update<T, B, GS_REORTH>(nv, S.vgrid, s, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
+                                    S.ldv, S.cdev(), S.cdevf(), S.N, S.red(), cyc);
+  reduce_slots_kernel<<<dim3(nv + 1, S.nslot), 256, 0, s>>>(S.cred(), kRedBlocks, nv + 1, 0,
+                                                            S.dev(kGsH2), cyc);
+  gs_decide_kernel<<<dim3(1, S.nslot), 64, 0, s>>>(S.dev(), S.devf(), nv, 2, cyc);
+  launch_gs_update<T, B, GS_FINAL2>(nv, S.vgrid, s, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
+                                    S.ldv, S.cdev(), S.cdevf(), S.N, S.red(), cyc);
+  gmres_givens_kernel<<<1, S.nthr, 0, s>>>(c->imp.gm, P, h, S.nslot, j);
+  stamp(c, s, PROF_ORTHO, 0);
 }
 
-template <class T>
-void enqueue_ilu_factor(const Sys<T>& S) {
+// End of a restart cycle (slots whose solve runs): x += M^{-1} V y, r = b - A x, and the
+// restart decision; the next cycle's v_0 = r / |r|.
+template <class T, class B>
+void enqueue_cycle_end(const Sys<T, B>& S, cudaStream_t s, const GmresParam& P,
+                       const GmresHandles& h) {
   bes_ctx* c = S.c;
+  const GmresDev& g = c->imp.gm;
+  stamp(c, s, PROF_ORTHO, 1);
+  gmres_solve_y_kernel<<<1, S.nthr, 0, s>>>(g, S.nslot);
+  lincomb_kernel<T, B><<<S.vgrid, 256, 0, s>>>(S.vec(S.W), S.cbasis(0), S.ldv, g.jc,
+                                               cslots((const double*)g.y, (int64_t)kMaxRestart),
+                                               S.N, g.lin);
+  stamp(c, s, PROF_ORTHO, 0);
+  stamp(c, s, PROF_PRECOND, 1);
+  enqueue_precond(S, s, S.cvec(S.W), g.lin);
+  stamp(c, s, PROF_PRECOND, 0);
+  stamp(c, s, PROF_SPMV, 1);
+  add_kernel<T><<<S.vgrid, 256, 0, s>>>(S.vec(S.X), S.cvec(S.Z), S.N, g.lin);
+  enqueue_spmv(S, s, S.cvec(S.X), S.cvec(S.b), S.vec(S.W), g.lin);
+  stamp(c, s, PROF_SPMV, 0);
+  stamp(c, s, PROF_ORTHO, 1);
+  norm2_kernel<T><<<S.vgrid, 256, 0, s>>>(S.cvec(S.W), S.N, S.red(), g.lin);
+  reduce_slots_kernel<<<dim3(1, S.nslot), 256, 0, s>>>(S.cred(), kRedBlocks, 1, 0, S.dev(kGsR),
+                                                       g.lin);
+  gmres_restart_kernel<<<1, S.nthr, 0, s>>>(g, P, h, S.nslot, c->imp.guard_dev);
+  basis_start_kernel<T, B><<<S.vgrid, 256, 0, s>>>(S.basis(0), S.vec(S.Vx), S.cvec(S.W),
+                                                   cslots((const double*)g.sc, 8LL), S.N, g.cyc);
+  stamp(c, s, PROF_ORTHO, 0);
+}
+
+// Start of the linear solves of the slots taking the step: x = 0, beta = |b|, v_0 = b / beta.
+template <class T, class B>
+void enqueue_solve_init(const Sys<T, B>& S, cudaStream_t s, const GmresParam& P,
+                        const GmresHandles& h) {
+  bes_ctx* c = S.c;
+  const GmresDev& g = c->imp.gm;
+  const int32_t* act = c->imp.act;
+  stamp(c, s, PROF_ORTHO, 1);
+  zero_kernel<T><<<S.vgrid, 256, 0, s>>>(S.vec(S.X), S.N, act);
+  norm2_kernel<T><<<S.vgrid, 256, 0, s>>>(S.cvec(S.b), S.N, S.red(), act);
+  reduce_slots_kernel<<<dim3(1, S.nslot), 256, 0, s>>>(S.cred(), kRedBlocks, 1, 0, S.dev(kGsR), act);
+  gmres_init_kernel<<<1, S.nthr, 0, s>>>(g, P, h, S.nslot, act, c->nan_flag);
+  basis_start_kernel<T, B><<<S.vgrid, 256, 0, s>>>(S.basis(0), S.vec(S.Vx), S.cvec(S.b),
+                                                   cslots((const double*)g.sc, 8LL), S.N, g.lin);
+  stamp(c, s, PROF_ORTHO, 0);
+}
+
+// ---- assembly and factorisation, slot by slot ----------------------------------------------
+
+// Residual of every slot taking the step (explicit stage-0 kernels, slots on the grid's y
+// axis): local or global time step at the slot's CFL, face-side states, face fluxes.
+void enqueue_residual_all(bes_ctx* c, cudaStream_t s, const SlotHandles& hs, int on) {
+  const DevMesh& m = c->dm;
+  const int nslot = c->imp.nslot;
+  step_begin_kernel<<<1, 256, 0, s>>>(hs, on, nslot, c->imp.act, c->dtmin);
+  Params prm = c->prm;
+  prm.active = c->imp.act;
+  stamp(c, s, PROF_RESIDUAL, 1);
+  cell_recon_kernel<true, false><<<dim3(nblk(m.nc, kBlock), nslot), kBlock, 0, s>>>(
+      m, prm, c->U[c->cur], c->RS, c->rs_ld, c->dt, 0.0, c->opt.local_time_step, c->dtmin,
+      nullptr, nullptr, c->imp.cfl_dev);
+  face_flux_kernel<false><<<dim3(nblk(m.nf, kBlock), nslot), kBlock, 0, s>>>(
+      m, prm, c->RS, c->rs_ld, c->FA, nullptr, c->nan_flag);
+  stamp(c, s, PROF_RESIDUAL, 0);
+}
+
+// 16-bit block-scaled copies (precision 2; T is float there)
+template <class T>
+void enqueue_pack(cudaStream_t s, int nc, const T* src, int slot0, int nslots, void* H, float* sc) {
+  if constexpr (std::is_same<T, float>::value)
+    pack_blocks_kernel<<<dim3(nblk(nc, 256), nslots), 256, 0, s>>>(src, slot0, nc, (__half2*)H, sc);
+}
+
+// Slot k: first-order Jacobians, the assembled system with its right-hand side, the 16-bit
+// copies (precision 2) and the step's norms (into norms [15]: L2 of the right-hand side [5],
+// L2 of R [5], max of the right-hand side [5]).
+template <class T, class B>
+void enqueue_assembly(const Sys<T, B>& S, cudaStream_t s, int k, double* norms) {
+  bes_ctx* c = S.c;
+  const DevMesh& m = c->dm;
+  const bes_options& o = c->opt;
+  const int64_t nc = m.nc, nf = m.nf;
+  const int local = o.local_time_step;
+  const double* U = c->U[c->cur] + k * 5 * nc;
+  const double* dt = c->dt + k * nc;
+  const unsigned long long* dtmin = c->dtmin + k;
+  Params prm = c->prm;
+  prm.pinf_dev = c->pinf_dev + 6 * k;
+  prm.active = nullptr;
+  FaceLocal fl{c->imp.m_own, c->imp.m_nb};
+  T* A = S.A_of(k);
+  T* Dinv = S.Dinv_of(k);
+  double* red = c->imp.red + (int64_t)k * 64 * c->imp.red_ld;
+  stamp(c, s, PROF_JACOBIAN, 1);
+  face_jacobian_kernel<T><<<nblk(nf, 128), 128, 0, s>>>(m, prm, fl, U, dt, dtmin, local,
+                                                        o.jacobian_repeat, A, S.Dc);
+  stamp(c, s, PROF_JACOBIAN, 0);
+  stamp(c, s, PROF_ASSEMBLE, 1);
+  const int nb = nblk(nc, 128);
+  cell_assemble_kernel<T><<<nb, 128, 0, s>>>(m, c->FA + k * 5 * nf, dt, dtmin, local,
+                                             o.jacobian_repeat, S.Dc, A,
+                                             uses_ilu(c) ? nullptr : Dinv,
+                                             c->imp.rhs + k * 5 * nc, S.b + k * S.ldv, red);
+  if (S.packed) {
+    enqueue_pack(s, (int)nc, A, 0, 5, S.A16 + k * 65 * nc, S.As + k * 5 * nc);
+    if (!uses_ilu(c)) enqueue_pack(s, (int)nc, Dinv, 0, 1, S.D16 + k * 13 * nc, S.Ds + k * nc);
+  }
+  reduce_rows_kernel<<<15, 256, 0, s>>>(red, nb, 10, 1, norms);
+  stamp(c, s, PROF_ASSEMBLE, 0);
+}
+
+// Slot k: block-ILU(0) factorisation of a copy of A, stage by stage (the factorisation of the
+// stage's rows, then the inverses of their diagonal blocks), and its 16-bit copies.
+template <class T, class B>
+void enqueue_factor(const Sys<T, B>& S, cudaStream_t s, int k) {
+  bes_ctx* c = S.c;
+  if (!uses_ilu(c)) return;
   const SoaMesh& M = c->soa;
-  // the factors overwrite a copy: the Krylov products need the unfactored matrix
-  cudaMemcpyAsync(S.LU, S.A, (size_t)125 * S.nc * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
-  // per stage: the factorisation of its rows, then the inverses of their diagonal blocks (a
-  // separate kernel keeps the factorisation's registers free of the 5x10 elimination array)
-  for (int k = 0; k < M.n_stages; ++k) {
-    const int n = M.stage_off[k + 1] - M.stage_off[k];
+  const int64_t nc = S.nc;
+  T* LU = S.LU_of(k);
+  T* Dinv = S.Dinv_of(k);
+  stamp(c, s, PROF_ILU_FACTOR, 1);
+  copy_vec_kernel<T><<<dim3(kRedBlocks, 1), 256, 0, s>>>(slots(LU, 0), cslots((const T*)S.A_of(k), 0),
+                                                        125 * nc, nullptr);
+  for (int q = 0; q < M.n_stages; ++q) {
+    const int n = M.stage_off[q + 1] - M.stage_off[q];
     if (c->imp.use_colour_ranges) {
-      ilu_factor_kernel<T, true><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, nullptr, n, nullptr, S.LU,
-                                                                S.Dinv, M.stage_off[k]);
-      ilu_invert_kernel<T, true><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, nullptr, n, S.LU, S.Dinv,
-                                                                M.stage_off[k]);
+      ilu_factor_kernel<T, true><<<nblk(n, 128), 128, 0, s>>>(c->dm, nullptr, n, nullptr, LU, Dinv,
+                                                              M.stage_off[q]);
+      ilu_invert_kernel<T, true><<<nblk(n, 128), 128, 0, s>>>(c->dm, nullptr, n, LU, Dinv,
+                                                              M.stage_off[q]);
     } else {
-      ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
-                                                          n, c->imp.ilu_pos, S.LU, S.Dinv);
-      ilu_invert_kernel<T><<<nblk(n, 128), 128, 0, S.s>>>(c->dm, c->imp.stage_rows + M.stage_off[k],
-                                                          n, S.LU, S.Dinv);
+      ilu_factor_kernel<T><<<nblk(n, 128), 128, 0, s>>>(c->dm, c->imp.stage_rows + M.stage_off[q],
+                                                        n, c->imp.ilu_pos, LU, Dinv);
+      ilu_invert_kernel<T><<<nblk(n, 128), 128, 0, s>>>(c->dm, c->imp.stage_rows + M.stage_off[q],
+                                                        n, LU, Dinv);
     }
   }
   if (S.packed) {
-    enqueue_pack(S, S.LU, 1, 4, c->imp.LU16, c->imp.LUs);
-    enqueue_pack(S, S.Dinv, 0, 1, c->imp.D16, c->imp.Ds);
+    enqueue_pack(s, (int)nc, LU, 1, 4, S.LU16 + k * 52 * nc, S.LUs + k * 4 * nc);
+    enqueue_pack(s, (int)nc, Dinv, 0, 1, S.D16 + k * 13 * nc, S.Ds + k * nc);
   }
+  stamp(c, s, PROF_ILU_FACTOR, 0);
 }
 
-// Colour-range sweeps (ilu_colour_kernel) from `in` into S.Z: colours 1..C-2 forward, the last
-// colour's two solves fused, colours C-2..0 backward.
-template <class T>
-void enqueue_ilu_colour_sweeps(const Sys<T>& S, const T* in) {
-  bes_ctx* c = S.c;
-  const SoaMesh& M = c->soa;
-  const int C = M.n_stages;
-  const int s1 = M.stage_off[1];
-  auto range = [&](int k, int& r0, int& r1) { r0 = M.stage_off[k]; r1 = M.stage_off[k + 1]; };
-  int r0, r1;
-  if constexpr (std::is_same<T, float>::value) {
-    if (S.packed) {
-      for (int k = 1; k < C - 1; ++k) {
-        range(k, r0, r1);
-        ilu_colour_packed_kernel<true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-            c->dm, r0, r1, s1, S.LU16, S.LUs, S.D16, S.Ds, in, S.Z);
-      }
-      range(C - 1, r0, r1);
-      ilu_colour_packed_kernel<true, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-          c->dm, r0, r1, s1, S.LU16, S.LUs, S.D16, S.Ds, in, S.Z);
-      for (int k = C - 2; k >= 0; --k) {
-        range(k, r0, r1);
-        ilu_colour_packed_kernel<false, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-            c->dm, r0, r1, s1, S.LU16, S.LUs, S.D16, S.Ds, in, S.Z);
-      }
-      return;
+// ---- the step graph -------------------------------------------------------------------------
+
+// Device address of slot k's norms in the device array of step results.
+double* result_norms(StepResult* res, int k) {
+  return reinterpret_cast<double*>(reinterpret_cast<char*>(res + k) + offsetof(StepResult, norms));
+}
+
+// End every capture still open after a failure, so the streams are usable again.
+void abandon_capture(bes_ctx* c) {
+  cudaStream_t ss[3] = {c->imp.cap[1], c->imp.cap[0], c->stream};
+  for (cudaStream_t s : ss) {
+    cudaStreamCaptureStatus st;
+    if (s && cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
     }
   }
-  for (int k = 1; k < C - 1; ++k) {
-    range(k, r0, r1);
-    ilu_colour_kernel<T, true, false><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-        c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
+  cudaGetLastError();
+}
+
+template <class T, class B>
+int capture_step(bes_ctx* c, int prof, cudaGraph_t* out) {
+  Sys<T, B> S(c);
+  ImplicitBuffers& I = c->imp;
+  const bes_options& o = c->opt;
+  cudaStream_t s0 = c->stream, s1 = I.cap[0], s2 = I.cap[1];
+  IMP_TRY(c, cudaStreamBeginCapture(s0, cudaStreamCaptureModeRelaxed));
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  IMP_TRY(c, cudaStreamGetCaptureInfo(s0, &st, nullptr, &g, nullptr, nullptr, nullptr));
+  SlotHandles hs;
+  std::memset(&hs, 0, sizeof(hs));
+  for (int k = 0; k < S.nslot; ++k)
+    IMP_TRY(c, cudaGraphConditionalHandleCreate(&hs.h[k], g, 0, cudaGraphCondAssignDefault));
+  GmresHandles gh;
+  std::memset(&gh, 0, sizeof(gh));
+  gh.on = 1;
+  IMP_TRY(c, cudaGraphConditionalHandleCreate(&gh.loop, g, 0, cudaGraphCondAssignDefault));
+  for (int j = 0; j < o.gmres_restart; ++j)
+    IMP_TRY(c, cudaGraphConditionalHandleCreate(&gh.arn[j], g, 0, cudaGraphCondAssignDefault));
+  const GmresParam P{o.gmres_restart, o.linear_solver_max_iter, o.linear_solver_tol};
+  int rc;
+  enqueue_residual_all(c, s0, hs, 1);
+  for (int k = 0; k < S.nslot; ++k) {
+    if ((rc = begin_conditional(c, s0, s1, hs.h[k], cudaGraphCondTypeIf))) return rc;
+    enqueue_assembly(S, s1, k, result_norms(I.res, k));
+    enqueue_factor(S, s1, k);
+    if ((rc = end_conditional(c, s1, &I.nodes_slot[prof]))) return rc;
   }
-  range(C - 1, r0, r1);
-  ilu_colour_kernel<T, true, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(c->dm, r0, r1, s1, S.LU,
-                                                                       S.Dinv, in, S.Z);
-  for (int k = C - 2; k >= 0; --k) {
-    range(k, r0, r1);
-    ilu_colour_kernel<T, false, true><<<nblk(r1 - r0, 128), 128, 0, S.s>>>(
-        c->dm, r0, r1, s1, S.LU, S.Dinv, in, S.Z);
+  enqueue_solve_init(S, s0, P, gh);
+  if ((rc = begin_conditional(c, s0, s1, gh.loop, cudaGraphCondTypeWhile))) return rc;
+  for (int j = 0; j < o.gmres_restart; ++j) {
+    if ((rc = begin_conditional(c, s1, s2, gh.arn[j], cudaGraphCondTypeIf))) return rc;
+    enqueue_arnoldi(S, s2, j, P, gh);
+    if ((rc = end_conditional(c, s2, &I.nodes_arn[prof]))) return rc;
   }
+  enqueue_cycle_end(S, s1, P, gh);
+  if ((rc = end_conditional(c, s1, &I.nodes_loop[prof]))) return rc;
+  gmres_finish_kernel<<<1, S.nthr, 0, s0>>>(I.gm, I.res, S.nslot, I.act);
+  stamp(c, s0, PROF_OTHER, 1);
+  state_update_kernel<T><<<S.vgrid, 256, 0, s0>>>(slots(c->U[c->cur], 5LL * S.nc), S.cvec(S.X),
+                                                  (int64_t)S.nc, c->nan_flag, I.act);
+  stamp(c, s0, PROF_OTHER, 0);
+  IMP_TRY(c, cudaGetLastError());
+  IMP_TRY(c, cudaStreamEndCapture(s0, out));
+  I.nodes_top[prof] = kernel_nodes(*out);
+  return BES_OK;
+}
+
+template <class T, class B>
+int build_step_graph(bes_ctx* c, int prof) {
+  ImplicitBuffers& I = c->imp;
+  if (!I.cap[0]) {
+    IMP_TRY(c, cudaStreamCreateWithFlags(&I.cap[0], cudaStreamNonBlocking));
+    IMP_TRY(c, cudaStreamCreateWithFlags(&I.cap[1], cudaStreamNonBlocking));
+  }
+  cudaGraph_t g = nullptr;
+  t_stamps = prof != 0;
+  const int rc = capture_step<T, B>(c, prof, &g);
+  t_stamps = false;
+  if (rc) {
+    abandon_capture(c);
+    return rc;
+  }
+  const cudaError_t e = cudaGraphInstantiate(&I.step_graph[prof][c->cur], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    c->last_error = std::string("cudaGraphInstantiate (implicit step): ") + cudaGetErrorString(e);
+    I.step_graph[prof][c->cur] = nullptr;
+    return BES_ERR_CUDA;
+  }
+  return BES_OK;
+}
+
+// ---- host side of a step -------------------------------------------------------------------
+
+double cfl_for_step(const bes_options& o, const SlotCtl& k) {
+  if (o.cfl_ramp_steps > 0) {
+    if (k.step_count >= o.cfl_ramp_steps - 1 || o.cfl_ramp_steps == 1) return o.cfl_ramp_end;
+    const double t = (double)k.step_count / (double)(o.cfl_ramp_steps - 1);
+    return o.cfl_ramp_start * std::pow(o.cfl_ramp_end / o.cfl_ramp_start, t);
+  }
+  return k.cfl_actual;
+}
+
+int check_step_nan(bes_ctx* c, int flag) {
+  if (!flag) return BES_OK;
+  IMP_TRY(c, cudaMemsetAsync(c->nan_flag, 0, sizeof(int), c->stream));
+  IMP_TRY(c, cudaStreamSynchronize(c->stream));
+  const int64_t f = c->soa.face_new2ref[flag - 1];
+  char buf[256];
+  std::snprintf(buf, sizeof(buf),
+                "NaN values encountered in flux across face %lld at coordinates [%e, %e, %e]",
+                (long long)f, c->ref.center[f * 3], c->ref.center[f * 3 + 1],
+                c->ref.center[f * 3 + 2]);
+  c->last_error = buf;
+  return BES_ERR_NAN;
+}
+
+// Upload the step's per-slot inputs: which slots step, their CFL and ramped freestream.
+int upload_step_inputs(bes_ctx* c, std::vector<int32_t>& act, std::vector<double>& cfl,
+                       std::vector<double>& P) {
+  ImplicitBuffers& I = c->imp;
+  const int ns = I.nslot;
+  act.assign(ns, 0);
+  cfl.assign(ns, 0.0);
+  P.assign(6 * ns, 0.0);
+  for (int k = 0; k < ns; ++k) {
+    act[k] = c->active_host[k] ? 1 : 0;
+    const SlotCtl& t = I.ctl[k];
+    cfl[k] = cfl_for_step(c->opt, t);
+    // FREESTREAM_RAMP (Config::getFreestreamPrimitiveVariables, src/Config.cpp:688-706)
+    freestream_from(&c->pinf0_host[6 * k], c->prm.ramp_steps, c->prm.ramp_frac, t.host_step,
+                    &P[6 * k]);
+  }
+  IMP_TRY(c, cudaMemcpyAsync(I.act, act.data(), ns * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  IMP_TRY(c, cudaMemcpyAsync(I.cfl_dev, cfl.data(), ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  IMP_TRY(c, cudaMemcpyAsync(c->pinf_dev, P.data(), P.size() * sizeof(double),
+                             cudaMemcpyHostToDevice, c->stream));
+  return BES_OK;
+}
+
+// n implicit steps of every active slot; history [n][nslot][19]
+template <class T, class B>
+int run_steps(bes_ctx* c, int64_t n, double* history) {
+  ImplicitBuffers& I = c->imp;
+  const bes_options& o = c->opt;
+  const int prof = c->prof.on ? 1 : 0;
+  const int ns = I.nslot;
+  if (!I.step_graph[prof][c->cur]) {
+    const int rc = build_step_graph<T, B>(c, prof);
+    if (rc) return rc;
+  }
+  std::vector<int32_t> act;
+  std::vector<double> cfl, P;
+  for (int64_t i = 0; i < n; ++i) {
+    int rc = upload_step_inputs(c, act, cfl, P);
+    if (rc) return rc;
+    IMP_TRY(c, cudaGraphLaunch(I.step_graph[prof][c->cur], c->stream));
+    int nan = 0;
+    unsigned long long cnt[2];
+    IMP_TRY(c, cudaMemcpyAsync(I.res_host.data(), I.res, ns * sizeof(StepResult),
+                               cudaMemcpyDeviceToHost, c->stream));
+    IMP_TRY(c, cudaMemcpyAsync(cnt, I.gm.counters, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+    IMP_TRY(c, cudaMemcpyAsync(&nan, c->nan_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    IMP_TRY(c, cudaStreamSynchronize(c->stream));
+    ++I.host_syncs;
+    // kernels this step launched: the graph's top level, the assembly of each slot that
+    // stepped, and the Arnoldi and restart-cycle bodies the device ran
+    int nact = 0;
+    for (int k = 0; k < ns; ++k) nact += act[k];
+    c->launches += I.nodes_top[prof] + nact * I.nodes_slot[prof] +
+                   (int64_t)(cnt[0] - I.counters_host[0]) * I.nodes_arn[prof] +
+                   (int64_t)(cnt[1] - I.counters_host[1]) * I.nodes_loop[prof];
+    I.counters_host[0] = cnt[0];
+    I.counters_host[1] = cnt[1];
+    if ((rc = check_step_nan(c, nan))) return rc;
+    int status = BES_OK;
+    for (int k = 0; k < ns; ++k) {
+      double* h = history ? history + (i * ns + k) * 19 : nullptr;
+      if (h) std::fill(h, h + 19, 0.0);
+      if (!act[k]) continue;
+      const StepResult& r = I.res_host[k];
+      SlotCtl& t = I.ctl[k];
+      // reduced rows: L2 of the right-hand side [5], L2 of R [5], max of the right-hand side [5]
+      double norms[15];
+      for (int v = 0; v < 5; ++v) {
+        norms[v] = r.norms[v];
+        norms[5 + v] = r.norms[10 + v];
+        norms[10 + v] = r.norms[5 + v];
+      }
+      for (int v = 0; v < 5; ++v) {
+        t.maxres_old[v] = t.maxres[v];
+        t.maxres[v] = norms[5 + v];
+      }
+      if (o.cfl_ramp_steps <= 0 && o.adaptive_courant_num_max > o.courant_num) {
+        // SolverImplicit::adaptCourantNum_ (src/SolverImplicit.cpp:530-550)
+        const int idx = (t.maxres_old[0] > t.maxres[0]) ? 1 : 0;
+        t.cfl_actual *= std::pow(t.maxres_old[0] / t.maxres[0], o.adaptive_courant_num_exponent[idx]);
+        t.cfl_actual = std::max(o.courant_num, t.cfl_actual);
+        t.cfl_actual = std::min(o.adaptive_courant_num_max, t.cfl_actual);
+      }
+      I.last_iters = r.iters;
+      I.last_err = r.rel;
+      I.total_lin_iters += r.iters;
+      I.gs_second_passes += r.second;
+      if (r.status != BES_OK) status = r.status;
+      if (h) {
+        for (int q = 0; q < 10; ++q) h[q] = norms[q];
+        h[10] = cfl[k];
+        h[11] = t.cfl_actual;
+        h[12] = r.iters;
+        h[13] = r.rel;
+        for (int q = 0; q < 5; ++q) h[14 + q] = norms[10 + q];
+      }
+      ++t.step_count;
+      ++t.host_step;
+    }
+    ++I.step_count;
+    if (status != BES_OK) {
+      c->last_error = "a linear solve was stopped after its restart-cycle limit";
+      return status;
+    }
+  }
+  return BES_OK;
+}
+
+template <class T>
+int run_steps_t(bes_ctx* c, int64_t n, double* history) {
+  if constexpr (std::is_same<T, float>::value)
+    if (c->imp.basis16) return run_steps<float, __half>(c, n, history);
+  return run_steps<T, T>(c, n, history);
+}
+
+// Residual and assembled system of slot 0 at the current state and the given CFL, without a
+// graph (bes_implicit_assemble).
+template <class T>
+int assemble_once(bes_ctx* c, double cfl, double* norms15) {
+  ImplicitBuffers& I = c->imp;
+  std::vector<int32_t> act(I.nslot, 0);
+  act[0] = 1;
+  std::vector<double> cf(I.nslot, cfl), P(6 * I.nslot, 0.0);
+  freestream_from(&c->pinf0_host[0], c->prm.ramp_steps, c->prm.ramp_frac, I.ctl[0].host_step, &P[0]);
+  IMP_TRY(c, cudaMemcpyAsync(I.act, act.data(), act.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  IMP_TRY(c, cudaMemcpyAsync(I.cfl_dev, cf.data(), cf.size() * 8, cudaMemcpyHostToDevice, c->stream));
+  IMP_TRY(c, cudaMemcpyAsync(c->pinf_dev, P.data(), P.size() * 8, cudaMemcpyHostToDevice, c->stream));
+  SlotHandles hs;
+  std::memset(&hs, 0, sizeof(hs));
+  enqueue_residual_all(c, c->stream, hs, 0);
+  Sys<T, T> S(c);
+  enqueue_assembly(S, c->stream, 0, result_norms(I.res, 0));
+  IMP_TRY(c, cudaGetLastError());
+  IMP_TRY(c, cudaMemcpyAsync(I.res_host.data(), I.res, sizeof(StepResult), cudaMemcpyDeviceToHost,
+                             c->stream));
+  int nan = 0;
+  IMP_TRY(c, cudaMemcpyAsync(&nan, c->nan_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  IMP_TRY(c, cudaStreamSynchronize(c->stream));
+  const double* r = I.res_host[0].norms;
+  for (int v = 0; v < 5; ++v) {
+    norms15[v] = r[v];
+    norms15[5 + v] = r[10 + v];
+    norms15[10 + v] = r[5 + v];
+  }
+  return check_step_nan(c, nan);
 }
 
 // True when the factorisation order is the identity and every stage is a contiguous range of
@@ -223,441 +718,36 @@ inline bool colour_ranges(const SoaMesh& M) {
   return true;
 }
 
-// Capture the stage-by-stage ILU work once per context as CUDA graphs (hundreds of small
-// kernels under level scheduling).  With colour ranges there is one sweep graph per input
-// vector (the Krylov vectors V_0..V_m and W), so that no copy of the input is needed.
-template <class T>
-int ensure_ilu_graphs(const Sys<T>& S) {
-  bes_ctx* c = S.c;
-  if (c->imp.apply_graph || !c->imp.colour_graphs.empty()) return BES_OK;
-  cudaGraph_t g;
-  IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
-  enqueue_ilu_factor(S);
-  IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
-  IMP_TRY(c, cudaGraphInstantiate(&c->imp.factor_graph, g, 0));
-  cudaGraphDestroy(g);
-  if (c->imp.use_colour_ranges) {
-    // inputs V_0..V_m, then W; with an FP16 basis the FP32 copy Vx, then W
-    const int nin = S.basis16 ? 2 : c->opt.gmres_restart + 2;
-    for (int q = 0; q < nin; ++q) {
-      const T* in = q + 1 < nin ? (S.basis16 ? S.Vx : S.Vk(q)) : S.W;
-      IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
-      enqueue_ilu_colour_sweeps(S, in);
-      IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
-      cudaGraphExec_t ge = nullptr;
-      IMP_TRY(c, cudaGraphInstantiate(&ge, g, 0));
-      cudaGraphDestroy(g);
-      c->imp.colour_graphs.push_back(ge);
-    }
-    return BES_OK;
-  }
-  IMP_TRY(c, cudaStreamBeginCapture(S.s, cudaStreamCaptureModeThreadLocal));
-  enqueue_ilu_sweeps(S);
-  IMP_TRY(c, cudaStreamEndCapture(S.s, &g));
-  IMP_TRY(c, cudaGraphInstantiate(&c->imp.apply_graph, g, 0));
-  cudaGraphDestroy(g);
-  return BES_OK;
-}
-
-// out = M^{-1} in (out is always S.Z)
-template <class T>
-void precond_apply(const Sys<T>& S, const T* in, T* out) {
-  bes_ctx* c = S.c;
-  if (uses_ilu(c) && c->imp.use_colour_ranges) {
-    // out is S.Z; in is one of V_0..V_m (graph q = its index) or Vx (graph 0), or W (the
-    // last graph)
-    const int64_t q = in == S.W ? (int64_t)c->imp.colour_graphs.size() - 1
-                                : (S.basis16 ? 0 : (in - S.V) / S.ldv);
-    cudaGraphLaunch(c->imp.colour_graphs[q], S.s);
-    c->launches += 2 * c->soa.n_stages - 1;
-  } else if (uses_ilu(c)) {
-    if (in != out)
-      cudaMemcpyAsync(out, in, (size_t)S.N * sizeof(T), cudaMemcpyDeviceToDevice, S.s);
-    cudaGraphLaunch(c->imp.apply_graph, S.s);
-    c->launches += 2 * c->soa.n_stages;
-  } else {
-    if constexpr (std::is_same<T, float>::value) {
-      if (S.packed) {
-        jacobi_apply_packed_kernel<<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, S.D16, S.Ds, in, out);
-        ++S.c->launches;
-        return;
-      }
-    }
-    jacobi_apply_kernel<T><<<nblk(S.nc, 256), 256, 0, S.s>>>(S.nc, S.Dinv, in, out);
-    ++S.c->launches;
-  }
-}
-
-template <class T>
-int precond_setup(const Sys<T>& S) {
-  bes_ctx* c = S.c;
-  if (!uses_ilu(c)) return BES_OK;  // block Jacobi inverted during assembly
-  int rc = ensure_ilu_graphs(S);
-  if (rc) return rc;
-  prof_begin(c, PROF_ILU_FACTOR);
-  IMP_TRY(c, cudaGraphLaunch(c->imp.factor_graph, S.s));
-  prof_end(c, PROF_ILU_FACTOR);
-  c->launches += 2 * c->soa.n_stages + (S.packed ? 2 : 0);
-  return BES_OK;
-}
-
-// Residual, first-order Jacobians and the assembled system at the current state; returns the
-// FP64 norms: L2[5] and max[5] of the Dt/V-scaled right-hand side, L2[5] of the residual R.
-template <class T>
-int assemble(bes_ctx* c, double cfl, double* norms15) {
-  Sys<T> S(c);
-  const DevMesh& m = c->dm;
-  const bes_options& o = c->opt;
-  const int local = o.local_time_step;
-  double* U = c->U[c->cur];
-  prof_begin(c, PROF_RESIDUAL);
-  reset_dtmin_kernel<<<1, 1, 0, S.s>>>(c->dtmin);
-  ++S.c->launches;
-  cell_recon_kernel<true, false><<<nblk(m.nc, kBlock), kBlock, 0, S.s>>>(
-      m, c->prm, U, c->RS, c->rs_ld, c->dt, cfl, local, c->dtmin, nullptr, nullptr);
-  ++S.c->launches;
-  face_flux_kernel<false><<<nblk(m.nf, kBlock), kBlock, 0, S.s>>>(m, c->prm, c->RS, c->rs_ld,
-                                                                  c->FA, nullptr, c->nan_flag);
-  ++S.c->launches;
-  prof_end(c, PROF_RESIDUAL);
-  FaceLocal fl{c->imp.m_own, c->imp.m_nb};
-  prof_begin(c, PROF_JACOBIAN);
-  face_jacobian_kernel<T><<<nblk(m.nf, 128), 128, 0, S.s>>>(
-      m, c->prm, fl, U, c->dt, c->dtmin, local, o.jacobian_repeat, S.A, S.Dc);
-  ++S.c->launches;
-  prof_end(c, PROF_JACOBIAN);
-  const int nb = nblk(m.nc, 128);
-  prof_begin(c, PROF_ASSEMBLE);
-  cell_assemble_kernel<T><<<nb, 128, 0, S.s>>>(m, c->FA, c->dt, c->dtmin, local,
-                                               o.jacobian_repeat, S.Dc, S.A,
-                                               uses_ilu(c) ? nullptr : S.Dinv,
-                                               c->imp.rhs, S.b, c->imp.red);
-  ++S.c->launches;
-  if (S.packed) {
-    enqueue_pack(S, S.A, 0, 5, c->imp.A16, c->imp.As);
-    if (!uses_ilu(c)) enqueue_pack(S, S.Dinv, 0, 1, c->imp.D16, c->imp.Ds);
-  }
-  prof_end(c, PROF_ASSEMBLE);
-  IMP_TRY(c, cudaGetLastError());
-  double r[15];
-  const int rc = reduce_to_host(c, 15, nb, 10, 1, r);
-  prof_collect(c);
-  // norms15: L2 of the right-hand side [5], max of the right-hand side [5], L2 of R [5]
-  for (int v = 0; v < 5; ++v) {
-    norms15[v] = r[v];
-    norms15[5 + v] = r[10 + v];
-    norms15[10 + v] = r[5 + v];
-  }
-  return rc;
-}
-
-// Right-preconditioned GMRES(m), x0 = 0, classical Gram-Schmidt with a conditional second
-// pass, Givens rotations; stops when |g_{j+1}| <= tol |b| (AMGCL gmres.hpp:163,214 semantics).
-template <class T, class B>
-int gmres_basis(bes_ctx* c, int& iters_out, double& rel_out) {
-  Sys<T> S(c);
-  constexpr bool kBasis16 = !std::is_same<T, B>::value;
-  B* const Vb = (B*)c->imp.V;
-  auto Vk = [&](int k) { return Vb + (int64_t)k * S.ldv; };
-  // the preconditioner's input: the basis vector itself, or its FP32 copy
-  auto pin = [&](int k) -> const T* {
-    if constexpr (kBasis16) return S.Vx;
-    else return Vk(k);
-  };
-  const bes_options& o = c->opt;
-  const int mr = o.gmres_restart;
-  const int maxiter = o.linear_solver_max_iter;
-  const double tol = o.linear_solver_tol;
-  const int G = kRedBlocks;
-  double* red = c->imp.red;
-  zero_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.N);
-  ++S.c->launches;
-  norm2_kernel<T><<<G, 256, 0, S.s>>>(S.b, S.N, red);
-  ++S.c->launches;
-  double norm_b2;
-  int rc = reduce_to_host(c, 1, G, 1, 0, &norm_b2);
-  if (rc) return rc;
-  const double norm_b = std::sqrt(norm_b2);
-  iters_out = 0;
-  rel_out = 0.0;
-  if (norm_b == 0.0) return BES_OK;
-  const double eps = tol * norm_b;
-  std::vector<double> H((mr + 1) * mr, 0.0), cs(mr), sn(mr), g(mr + 1), y(mr);
-  int iter = 0;
-  double norm_r = norm_b;
-  scale_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.b, 1.0, S.N);  // r = b
-  double beta = norm_b;
-  ++S.c->launches;
-  while (true) {
-    if (beta < eps || iter >= maxiter) break;
-    if constexpr (kBasis16)
-      basis_start_kernel<<<G, 256, 0, S.s>>>(Vk(0), S.Vx, S.W, 1.0 / beta, S.N);
-    else
-      scale_kernel<T><<<G, 256, 0, S.s>>>(Vk(0), S.W, 1.0 / beta, S.N);
-    ++S.c->launches;
-    std::fill(g.begin(), g.end(), 0.0);
-    g[0] = beta;
-    int j = 0;
-    while (j < mr && iter < maxiter) {
-      prof_begin(c, PROF_PRECOND);
-      precond_apply(S, pin(j), S.Z);
-      prof_end(c, PROF_PRECOND);
-      prof_begin(c, PROF_SPMV);
-      spmv<T>(S, S.Z, nullptr, S.W);
-      prof_end(c, PROF_SPMV);
-      // classical Gram-Schmidt with a conditional second pass (gs_* kernels); the
-      // coefficients stay on the device and reach the host once per iteration
-      double* dev = c->imp.red_out;
-      const int nv = j + 1;
-      prof_begin(c, PROF_ORTHO);
-      T* const vx = kBasis16 ? S.Vx : nullptr;
-      launch_gs_dots<T, B>(nv, G, S.s, Vb, S.ldv, S.W, S.N, red);
-      reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev);
-      float* devf = c->imp.red_out_f;
-      gs_decide_kernel<<<1, 64, 0, S.s>>>(dev, devf, nv, 1);
-      launch_gs_update<T, B, GS_FINAL1>(nv, G, S.s, Vk(j + 1), vx, S.W, Vb, S.ldv, dev, devf,
-                                        S.N, red);
-      launch_gs_update<T, B, GS_REORTH>(nv, G, S.s, nullptr, nullptr, S.W, Vb, S.ldv, dev, devf,
-                                        S.N, red);
-      reduce_rows_kernel<<<nv + 1, 256, 0, S.s>>>(red, G, nv + 1, 0, dev + kGsH2);
-      gs_decide_kernel<<<1, 64, 0, S.s>>>(dev, devf, nv, 2);
-      launch_gs_update<T, B, GS_FINAL2>(nv, G, S.s, Vk(j + 1), vx, S.W, Vb, S.ldv, dev, devf,
-                                        S.N, red);
-      prof_end(c, PROF_ORTHO);
-      S.c->launches += 8;
-      double hbuf[kGsScalars];
-      IMP_TRY(c, cudaMemcpyAsync(hbuf, dev, sizeof(hbuf), cudaMemcpyDeviceToHost, S.s));
-      IMP_TRY(c, cudaStreamSynchronize(S.s));
-      prof_collect(c);
-      const bool second = hbuf[kGsFlag] != 0.0;
-      if (second) ++c->imp.gs_second_passes;
-      for (int i = 0; i <= j; ++i) H[i * mr + j] = hbuf[i] + (second ? hbuf[kGsH2 + i] : 0.0);
-      H[(j + 1) * mr + j] = hbuf[kGsNorm];
-      for (int i = 0; i < j; ++i) {
-        const double t = cs[i] * H[i * mr + j] + sn[i] * H[(i + 1) * mr + j];
-        H[(i + 1) * mr + j] = -sn[i] * H[i * mr + j] + cs[i] * H[(i + 1) * mr + j];
-        H[i * mr + j] = t;
-      }
-      const double a = H[j * mr + j], cc = H[(j + 1) * mr + j];
-      const double d = std::sqrt(a * a + cc * cc);
-      cs[j] = (d == 0.0) ? 1.0 : a / d;
-      sn[j] = (d == 0.0) ? 0.0 : cc / d;
-      H[j * mr + j] = d;
-      H[(j + 1) * mr + j] = 0.0;
-      g[j + 1] = -sn[j] * g[j];
-      g[j] = cs[j] * g[j];
-      ++j;
-      ++iter;
-      if (std::fabs(g[j]) <= eps) break;
-    }
-    for (int i = j - 1; i >= 0; --i) {
-      double s = g[i];
-      for (int k = i + 1; k < j; ++k) s -= H[i * mr + k] * y[k];
-      y[i] = s / H[i * mr + i];
-    }
-    IMP_TRY(c, cudaMemcpyAsync(c->imp.coef, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, S.s));
-    lincomb_kernel<T, B><<<G, 256, 0, S.s>>>(S.W, Vb, S.ldv, j, c->imp.coef, S.N);
-    ++S.c->launches;
-    precond_apply(S, S.W, S.Z);
-    add_kernel<T><<<G, 256, 0, S.s>>>(S.X, S.Z, S.N);
-    ++S.c->launches;
-    spmv<T>(S, S.X, S.b, S.W);  // r = b - A x
-    norm2_kernel<T><<<G, 256, 0, S.s>>>(S.W, S.N, red);
-    ++S.c->launches;
-    double nr2;
-    if ((rc = reduce_to_host(c, 1, G, 1, 0, &nr2))) return rc;
-    norm_r = std::sqrt(nr2);
-    if (norm_r <= eps || iter >= maxiter) break;
-    beta = norm_r;
-  }
-  iters_out = iter;
-  rel_out = norm_r / norm_b;
-  IMP_TRY(c, cudaGetLastError());
-  return BES_OK;
-}
-
-template <class T>
-int gmres(bes_ctx* c, int& iters_out, double& rel_out) {
-  if constexpr (std::is_same<T, float>::value)
-    if (c->imp.basis16) return gmres_basis<float, __half>(c, iters_out, rel_out);
-  return gmres_basis<T, T>(c, iters_out, rel_out);
-}
-
-double cfl_for_step(const bes_ctx* c) {
-  const bes_options& o = c->opt;
-  if (o.cfl_ramp_steps > 0) {
-    const int64_t k = c->imp.step_count;
-    if (k >= o.cfl_ramp_steps - 1 || o.cfl_ramp_steps == 1) return o.cfl_ramp_end;
-    const double t = (double)k / (double)(o.cfl_ramp_steps - 1);
-    return o.cfl_ramp_start * std::pow(o.cfl_ramp_end / o.cfl_ramp_start, t);
-  }
-  return c->imp.cfl_actual;
-}
-
-template <class T>
-int implicit_step(bes_ctx* c, double* hist) {
-  ImplicitBuffers& I = c->imp;
-  const bes_options& o = c->opt;
-  for (int v = 0; v < 5; ++v) I.maxres_old[v] = I.maxres[v];
-  const double cfl = cfl_for_step(c);
-  double P[6];
-  freestream_at(c->prm, c->host_step, P);  // FREESTREAM_RAMP
-  IMP_TRY(c, cudaMemcpyAsync(c->pinf_dev, P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
-  double norms[15];
-  int rc = assemble<T>(c, cfl, norms);
-  if (rc) return rc;
-  rc = check_nan_public(c);
-  if (rc) return rc;
-  Sys<T> S(c);
-  rc = precond_setup(S);
-  if (rc) return rc;
-  int iters = 0;
-  double rel = 0.0;
-  rc = gmres<T>(c, iters, rel);
-  if (rc) return rc;
-  prof_begin(c, PROF_OTHER);
-  state_update_kernel<T><<<kRedBlocks, 256, 0, c->stream>>>(c->U[c->cur], S.X, (int64_t)S.nc);
-  prof_end(c, PROF_OTHER);
-  ++c->launches;
-  IMP_TRY(c, cudaGetLastError());
-  for (int v = 0; v < 5; ++v) I.maxres[v] = norms[5 + v];
-  if (o.cfl_ramp_steps <= 0 && o.adaptive_courant_num_max > o.courant_num) {
-    // SolverImplicit::adaptCourantNum_ (src/SolverImplicit.cpp:530-550)
-    const int idx = (I.maxres_old[0] > I.maxres[0]) ? 1 : 0;
-    I.cfl_actual *= std::pow(I.maxres_old[0] / I.maxres[0], o.adaptive_courant_num_exponent[idx]);
-    I.cfl_actual = std::max(o.courant_num, I.cfl_actual);
-    I.cfl_actual = std::min(o.adaptive_courant_num_max, I.cfl_actual);
-  }
-  I.last_iters = iters;
-  I.total_lin_iters += iters;
-  I.last_err = rel;
-  if (hist) {
-    for (int k = 0; k < 10; ++k) hist[k] = norms[k];
-    hist[10] = cfl;
-    hist[11] = I.cfl_actual;
-    hist[12] = iters;
-    hist[13] = rel;
-    for (int k = 0; k < 5; ++k) hist[14 + k] = norms[10 + k];
-  }
-  ++I.step_count;
-  ++c->host_step;
-  return BES_OK;
-}
-
-// A batched context's condition b seen as a single-condition context: its state, face
-// states, fluxes, time steps and freestream, and its CFL controller, swapped in for the
-// duration of one implicit step (the implicit buffers are shared by all conditions).
-struct ConditionView {
-  bes_ctx* c;
-  double* U[2];
-  double *RS, *FA, *dt, *pinf;
-  unsigned long long* dtmin;
-  Params prm;
-  bes_ctx::CondImplicit saved;
-  int nb;
-  ConditionView(bes_ctx* ctx, int b) : c(ctx) {
-    const int64_t nc = c->soa.nc, nf = c->soa.nf;
-    for (int k = 0; k < 2; ++k) U[k] = c->U[k];
-    RS = c->RS; FA = c->FA; dt = c->dt; pinf = c->pinf_dev; dtmin = c->dtmin;
-    prm = c->prm;
-    nb = c->nb;
-    for (int k = 0; k < 2; ++k) c->U[k] += (int64_t)b * 5 * nc;
-    c->RS += (int64_t)b * 5 * c->rs_ld;
-    c->FA += (int64_t)b * 5 * nf;
-    c->dt += (int64_t)b * nc;
-    c->dtmin += b;
-    c->pinf_dev += 6 * b;
-    c->prm.pinf_dev = c->pinf_dev;
-    c->prm.active = nullptr;
-    for (int i = 0; i < 6; ++i) c->prm.pinf[i] = c->pinf0_host[6 * b + i];
-    c->nb = 1;
-    swap_scalars(c->cond_imp[b]);
-  }
-  void swap_scalars(bes_ctx::CondImplicit& s) {
-    ImplicitBuffers& I = c->imp;
-    std::swap(s.cfl_actual, I.cfl_actual);
-    for (int v = 0; v < 5; ++v) {
-      std::swap(s.maxres[v], I.maxres[v]);
-      std::swap(s.maxres_old[v], I.maxres_old[v]);
-    }
-    std::swap(s.step_count, I.step_count);
-    std::swap(s.host_step, c->host_step);
-  }
-  void release(int b) {
-    swap_scalars(c->cond_imp[b]);
-    for (int k = 0; k < 2; ++k) c->U[k] = U[k];
-    c->RS = RS; c->FA = FA; c->dt = dt; c->pinf_dev = pinf; c->dtmin = dtmin;
-    c->prm = prm;
-    c->nb = nb;
-  }
-};
-
-// n implicit steps of every condition of a batch, condition after condition within a step;
-// history [n][nb][19]
-int implicit_steps_batch(bes_ctx* ctx, int64_t n, double* history) {
-  const int nb = ctx->nb;
-  for (int64_t i = 0; i < n; ++i) {
-    for (int b = 0; b < nb; ++b) {
-      ConditionView view(ctx, b);
-      double* h = history ? history + (i * nb + b) * 19 : nullptr;
-      const int rc = ctx->imp.prec ? implicit_step<float>(ctx, h) : implicit_step<double>(ctx, h);
-      view.release(b);
-      if (rc) return rc;
-    }
-    ++ctx->imp.step_count;
-    ++ctx->host_step;
-  }
-  IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  prof_collect(ctx);
-  return BES_OK;
-}
-
 }  // namespace
 
 namespace bes {
 
-void prof_begin(bes_ctx* c, int cat) {
-  Profiler& P = c->prof;
-  if (!P.on) return;
-  if (P.next * 2 + 2 > (int)P.pool.size()) {
-    for (int q = 0; q < 64; ++q) {
-      cudaEvent_t e;
-      cudaEventCreate(&e);
-      P.pool.push_back(e);
-    }
+void implicit_reset(bes_ctx* c) {
+  for (SlotCtl& k : c->imp.ctl) {
+    k = SlotCtl();
+    k.cfl_actual = c->opt.courant_num;
   }
-  const int pr = P.next++;
-  P.open_pair[cat] = pr;
-  cudaEventRecord(P.pool[2 * pr], c->stream);
 }
 
-void prof_end(bes_ctx* c, int cat) {
-  Profiler& P = c->prof;
-  if (!P.on) return;
-  const int pr = P.open_pair[cat];
-  cudaEventRecord(P.pool[2 * pr + 1], c->stream);
-  P.pending.push_back({cat, pr});
-}
-
-void prof_collect(bes_ctx* c) {
-  Profiler& P = c->prof;
-  if (!P.on) return;
-  cudaStreamSynchronize(c->stream);
-  for (auto& q : P.pending) {
-    float ms = 0;
-    if (cudaEventElapsedTime(&ms, P.pool[2 * q.second], P.pool[2 * q.second + 1]) == cudaSuccess) {
-      P.ms[q.first] += ms;
-      P.count[q.first] += 1;
+void implicit_release(bes_ctx* c) {
+  ImplicitBuffers& I = c->imp;
+  for (int p = 0; p < 2; ++p)
+    for (int q = 0; q < 2; ++q)
+      if (I.step_graph[p][q]) {
+        cudaGraphExecDestroy(I.step_graph[p][q]);
+        I.step_graph[p][q] = nullptr;
+      }
+  for (cudaStream_t& s : I.cap)
+    if (s) {
+      cudaStreamDestroy(s);
+      s = nullptr;
     }
-  }
-  P.pending.clear();
-  P.next = 0;
 }
 
 int implicit_allocate(bes_ctx* c) {
   ImplicitBuffers& I = c->imp;
   const bes_options& o = c->opt;
-  if (o.gmres_restart < 1 || o.gmres_restart > 32) {
+  if (o.gmres_restart < 1 || o.gmres_restart > kMaxRestart) {
     c->last_error = "GMRES_RESTART must be between 1 and 32";
     return BES_ERR_UNSUPPORTED;
   }
@@ -666,61 +756,94 @@ int implicit_allocate(bes_ctx* c) {
                     "16-bit block-scaled matrix storage)";
     return BES_ERR_UNSUPPORTED;
   }
-  I.prec = o.precision ? 1 : 0;
-  I.packed = o.precision == 2;
-  I.tsize = I.prec ? sizeof(float) : sizeof(double);
-  const SoaMesh& M = c->soa;
-  const int64_t nc = M.nc, nf = M.nf, N = 5 * nc;
-  int rc = 0;
-  rc |= imp_malloc(c, &I.A, 125 * nc * I.tsize);
-  rc |= imp_malloc(c, &I.Dinv, 25 * nc * I.tsize);
   if (o.linear_solver < 0 || o.linear_solver > 2) {
     c->last_error = "linear_solver must be 0 (block Jacobi), 1 (block ILU(0), colour order) or 2 "
                     "(block ILU(0), RCM order, level scheduled)";
     return BES_ERR_UNSUPPORTED;
   }
+  if (c->nb > kMaxSlots) {
+    c->last_error = "an implicit context holds at most 256 conditions";
+    return BES_ERR_UNSUPPORTED;
+  }
+  I.prec = o.precision ? 1 : 0;
+  I.packed = o.precision == 2;
+  I.basis16 = I.packed;
+  I.tsize = I.prec ? sizeof(float) : sizeof(double);
+  I.nslot = c->nb;
+  const SoaMesh& M = c->soa;
+  const int64_t nc = M.nc, nf = M.nf, ns = I.nslot;
   if (o.linear_solver == 2) build_ilu_schedule(c->soa, true);
   I.use_colour_ranges = o.linear_solver == 1 && colour_ranges(c->soa);
   if (I.packed && uses_ilu(c) && !I.use_colour_ranges) {
     c->last_error = "precision 2 runs block Jacobi or the colour-ordered block ILU(0)";
     return BES_ERR_UNSUPPORTED;
   }
-  if (uses_ilu(c)) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize);
+  I.ldv = basis_stride(nc);
+  // the system in T: per condition, or one scratch shared by all (16-bit storage)
+  const int64_t msl = I.packed ? 1 : ns;
+  I.sA = I.packed ? 0 : 125 * nc;
+  I.sDinv = I.packed ? 0 : 25 * nc;
+  int rc = 0;
+  rc |= imp_malloc(c, &I.A, 125 * nc * I.tsize * msl);
+  rc |= imp_malloc(c, &I.Dinv, 25 * nc * I.tsize * msl);
+  if (uses_ilu(c)) rc |= imp_malloc(c, &I.LU, 125 * nc * I.tsize * msl);
   if (I.packed) {
-    rc |= imp_malloc(c, &I.A16, 5 * 13 * nc * sizeof(__half2));
-    rc |= imp_malloc(c, (void**)&I.As, 5 * nc * sizeof(float));
-    rc |= imp_malloc(c, &I.D16, 13 * nc * sizeof(__half2));
-    rc |= imp_malloc(c, (void**)&I.Ds, nc * sizeof(float));
+    rc |= imp_malloc(c, &I.A16, 65 * nc * sizeof(__half2) * ns);
+    rc |= imp_malloc(c, (void**)&I.As, 5 * nc * sizeof(float) * ns);
+    rc |= imp_malloc(c, &I.D16, 13 * nc * sizeof(__half2) * ns);
+    rc |= imp_malloc(c, (void**)&I.Ds, nc * sizeof(float) * ns);
     if (uses_ilu(c)) {
-      rc |= imp_malloc(c, &I.LU16, 4 * 13 * nc * sizeof(__half2));
-      rc |= imp_malloc(c, (void**)&I.LUs, 4 * nc * sizeof(float));
+      rc |= imp_malloc(c, &I.LU16, 52 * nc * sizeof(__half2) * ns);
+      rc |= imp_malloc(c, (void**)&I.LUs, 4 * nc * sizeof(float) * ns);
     }
   }
   rc |= imp_malloc(c, &I.Dc, 50 * nf * I.tsize);
-  rc |= imp_malloc(c, &I.b, N * I.tsize);
-  I.basis16 = I.packed;
-  rc |= imp_malloc(c, &I.V, (size_t)(o.gmres_restart + 1) * basis_stride(nc) *
-                                (I.basis16 ? sizeof(__half) : I.tsize));
-  if (I.basis16) rc |= imp_malloc(c, &I.Vx, N * sizeof(float));
-  rc |= imp_malloc(c, &I.Z, N * I.tsize);
-  rc |= imp_malloc(c, &I.W, N * I.tsize);
-  rc |= imp_malloc(c, &I.X, N * I.tsize);
-  rc |= imp_malloc(c, (void**)&I.rhs, N * sizeof(double));
-  rc |= imp_malloc(c, (void**)&I.red, 64 * (size_t)std::max<int64_t>(kRedBlocks, nblk(nc, 128)) * sizeof(double));
-  rc |= imp_malloc(c, (void**)&I.red_out, 128 * sizeof(double));
-  rc |= imp_malloc(c, (void**)&I.red_out_f, 128 * sizeof(float));
-  rc |= imp_malloc(c, (void**)&I.coef, 64 * sizeof(double));
+  rc |= imp_malloc(c, &I.b, I.ldv * I.tsize * ns);
+  I.sV = (int64_t)(o.gmres_restart + 1) * I.ldv;
+  rc |= imp_malloc(c, &I.V, I.sV * (I.basis16 ? sizeof(__half) : I.tsize) * ns);
+  if (I.basis16) rc |= imp_malloc(c, &I.Vx, I.ldv * sizeof(float) * ns);
+  rc |= imp_malloc(c, &I.Z, I.ldv * I.tsize * ns);
+  rc |= imp_malloc(c, &I.W, I.ldv * I.tsize * ns);
+  rc |= imp_malloc(c, &I.X, I.ldv * I.tsize * ns);
+  rc |= imp_malloc(c, (void**)&I.rhs, 5 * nc * sizeof(double) * ns);
+  I.red_ld = std::max<int64_t>(kRedBlocks, nblk(nc, 128));
+  rc |= imp_malloc(c, (void**)&I.red, 64 * I.red_ld * sizeof(double) * ns);
+  GmresDev& g = I.gm;
+  rc |= imp_malloc(c, (void**)&g.H, ns * kHsize * sizeof(double));
+  rc |= imp_malloc(c, (void**)&g.cs, ns * kMaxRestart * sizeof(double));
+  rc |= imp_malloc(c, (void**)&g.sn, ns * kMaxRestart * sizeof(double));
+  rc |= imp_malloc(c, (void**)&g.g, ns * (kMaxRestart + 1) * sizeof(double));
+  rc |= imp_malloc(c, (void**)&g.y, ns * kMaxRestart * sizeof(double));
+  rc |= imp_malloc(c, (void**)&g.sc, ns * 8 * sizeof(double));
+  int32_t** ints[] = {&g.lin, &g.cyc, &g.jc, &g.iter, &g.second, &g.status, &g.cycles};
+  for (int32_t** p : ints) rc |= imp_malloc(c, (void**)p, ns * sizeof(int32_t));
+  rc |= imp_malloc(c, (void**)&g.dev, ns * kGsLd * sizeof(double));
+  rc |= imp_malloc(c, (void**)&g.devf, ns * kGsLd * sizeof(float));
+  rc |= imp_malloc(c, (void**)&g.counters, 2 * sizeof(unsigned long long));
+  rc |= imp_malloc(c, (void**)&I.res, ns * sizeof(StepResult));
+  rc |= imp_malloc(c, (void**)&I.cfl_dev, ns * sizeof(double));
+  rc |= imp_malloc(c, (void**)&I.act, ns * sizeof(int32_t));
+  rc |= imp_malloc(c, (void**)&I.guard_dev, sizeof(int32_t));
+  rc |= imp_malloc(c, (void**)&c->prof.dev, 3 * PROF_NCAT * sizeof(unsigned long long));
   rc |= imp_malloc(c, (void**)&I.m_own, nf);
   rc |= imp_malloc(c, (void**)&I.m_nb, nf);
   rc |= imp_malloc(c, (void**)&I.stage_rows, nc * sizeof(int32_t));
   rc |= imp_malloc(c, (void**)&I.ilu_pos, nc * sizeof(int32_t));
   if (rc) return BES_ERR_CUDA;
-  IMP_TRY(c, cudaMemset(I.A, 0, 125 * nc * I.tsize));  // empty slots stay zero
+  IMP_TRY(c, cudaMemset(I.A, 0, 125 * nc * I.tsize * msl));  // empty slots stay zero
+  IMP_TRY(c, cudaMemset(g.lin, 0, ns * sizeof(int32_t)));
+  IMP_TRY(c, cudaMemset(g.cyc, 0, ns * sizeof(int32_t)));
+  IMP_TRY(c, cudaMemset(g.counters, 0, 2 * sizeof(unsigned long long)));
+  IMP_TRY(c, cudaMemset(I.guard_dev, 0, sizeof(int32_t)));
+  IMP_TRY(c, cudaMemset(I.res, 0, ns * sizeof(StepResult)));
+  IMP_TRY(c, cudaMemset(c->prof.dev, 0, 3 * PROF_NCAT * sizeof(unsigned long long)));
   IMP_TRY(c, cudaMemcpy(I.m_own, M.f_m_own.data(), nf, cudaMemcpyHostToDevice));
   IMP_TRY(c, cudaMemcpy(I.m_nb, M.f_m_nb.data(), nf, cudaMemcpyHostToDevice));
   IMP_TRY(c, cudaMemcpy(I.stage_rows, M.stage_rows.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice));
   IMP_TRY(c, cudaMemcpy(I.ilu_pos, M.ilu_pos.data(), nc * sizeof(int32_t), cudaMemcpyHostToDevice));
-  I.cfl_actual = o.courant_num;
+  I.res_host.assign(ns, StepResult());
+  I.ctl.assign(ns, SlotCtl());
+  implicit_reset(c);
   return BES_OK;
 }
 
@@ -734,21 +857,22 @@ int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history) {
     ctx->last_error = "context was not created for the implicit solver";
     return BES_ERR_INVALID;
   }
-  if (ctx->nb > 1) return implicit_steps_batch(ctx, n, history);
-  for (int64_t i = 0; i < n; ++i) {
-    int rc = ctx->imp.prec ? implicit_step<float>(ctx, history ? history + i * 19 : nullptr)
-                           : implicit_step<double>(ctx, history ? history + i * 19 : nullptr);
-    if (rc) return rc;
-  }
-  IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  prof_collect(ctx);
-  return BES_OK;
+  return ctx->imp.prec ? run_steps_t<float>(ctx, n, history) : run_steps_t<double>(ctx, n, history);
 }
 
 int bes_profile(bes_ctx* ctx, int32_t enable, double* ms_out, int64_t* counts_out) {
   if (!ctx) return BES_ERR_INVALID;
   Profiler& P = ctx->prof;
-  prof_collect(ctx);
+  if (P.dev) {
+    unsigned long long h[3 * PROF_NCAT];
+    IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    IMP_TRY(ctx, cudaMemcpy(h, P.dev, sizeof(h), cudaMemcpyDeviceToHost));
+    IMP_TRY(ctx, cudaMemset(P.dev, 0, sizeof(h)));
+    for (int k = 0; k < PROF_NCAT; ++k) {
+      P.ms[k] = h[PROF_NCAT + k] * 1e-6;
+      P.count[k] = (int64_t)h[2 * PROF_NCAT + k];
+    }
+  }
   if (ms_out)
     for (int k = 0; k < PROF_NCAT; ++k) ms_out[k] = P.ms[k];
   if (counts_out)
@@ -758,6 +882,25 @@ int bes_profile(bes_ctx* ctx, int32_t enable, double* ms_out, int64_t* counts_ou
     P.count[k] = 0;
   }
   P.on = enable != 0;
+  return BES_OK;
+}
+
+int bes_implicit_stats(const bes_ctx* ctx, int64_t* out) {
+  if (!ctx || !out) return BES_ERR_INVALID;
+  out[0] = ctx->imp.step_count;
+  out[1] = ctx->imp.host_syncs;
+  out[2] = (int64_t)ctx->imp.counters_host[0];
+  out[3] = (int64_t)ctx->imp.counters_host[1];
+  return BES_OK;
+}
+
+int bes_set_linear_guard(bes_ctx* ctx, int32_t max_cycles) {
+  if (!ctx || max_cycles < 0) return BES_ERR_INVALID;
+  if (ctx->opt.solver_type != 1 || !ctx->imp.guard_dev) return BES_ERR_INVALID;
+  ctx->imp.guard = max_cycles;
+  IMP_TRY(ctx, cudaMemcpyAsync(ctx->imp.guard_dev, &ctx->imp.guard, sizeof(int32_t),
+                               cudaMemcpyHostToDevice, ctx->stream));
+  IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return BES_OK;
 }
 
@@ -779,9 +922,8 @@ int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks,
   if (n_blocks) *n_blocks = nb;
   if (!rhs && !blocks) return BES_OK;
   double norms[15];
-  int rc = ctx->imp.prec ? assemble<float>(ctx, cfl, norms) : assemble<double>(ctx, cfl, norms);
+  int rc = ctx->imp.prec ? assemble_once<float>(ctx, cfl, norms) : assemble_once<double>(ctx, cfl, norms);
   if (rc) return rc;
-  IMP_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   if (rhs) {
     std::vector<double> h(5 * nc);
     IMP_TRY(ctx, cudaMemcpy(h.data(), ctx->imp.rhs, 5 * nc * sizeof(double), cudaMemcpyDeviceToHost));
@@ -809,7 +951,7 @@ int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks,
       }
     }
   }
-  return check_nan_public(ctx);
+  return BES_OK;
 }
 
 int bes_ilu_order(bes_ctx* ctx, int64_t* order) {

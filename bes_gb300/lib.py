@@ -29,6 +29,7 @@ EXPORTED = [
     "bes_ilu_order", "bes_counters", "bes_wall_force", "bes_profile",
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
     "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
+    "bes_implicit_stats", "bes_set_linear_guard", "bes_set_condition",
     "bes_mlp_create", "bes_mlp_destroy", "bes_mlp_last_error", "bes_mlp_train", "bes_mlp_infer",
     "bes_mlp_init_state", "bes_mlp_params", "bes_mlp_features", "bes_mlp_loss_grad",
     "bes_mlp_apply_grad", "bes_mlp_normalisation",
@@ -137,6 +138,9 @@ def load(path: str = LIB_PATH):
     L.bes_set_active.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
     L.bes_sweep_run.argtypes = [P, ctypes.c_int64, ctypes.c_double, ctypes.c_int64,
                                 ctypes.POINTER(ctypes.c_int64), D]
+    L.bes_implicit_stats.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    L.bes_set_linear_guard.argtypes = [P, ctypes.c_int32]
+    L.bes_set_condition.argtypes = [P, ctypes.c_int32, D, D]
     F32 = ctypes.POINTER(ctypes.c_float)
     I64p = ctypes.POINTER(ctypes.c_int64)
     L.bes_mlp_create.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(P)]
@@ -417,8 +421,8 @@ class Context:
                           "spmv", "gram_schmidt", "update")
 
     def profile(self, enable: bool = True) -> dict:
-        """Turn implicit-path event timing on/off; returns what accumulated since the last call
-        as {category: (ms, count)}."""
+        """Turn implicit-path device timing on/off; returns what accumulated since the last
+        call as {category: (ms, count)}."""
         ms = np.zeros(8)
         cnt = np.zeros(8, np.int64)
         self._check(load().bes_profile(self.h, int(enable), _d(ms), _i(cnt)))
@@ -456,6 +460,25 @@ class Context:
         return dict(launches=int(out[0]), explicit_iterations=int(out[1]),
                     implicit_steps=int(out[2]), linear_iterations=int(out[3]),
                     gram_schmidt_second_passes=int(out[4]))
+
+    def implicit_stats(self) -> dict:
+        """bes_implicit_stats: steps, host synchronisations, Arnoldi steps and restart cycles
+        the device ran."""
+        out = np.zeros(4, np.int64)
+        self._check(load().bes_implicit_stats(self.h, _i(out)))
+        return dict(steps=int(out[0]), host_syncs=int(out[1]), arnoldi_steps=int(out[2]),
+                    restart_cycles=int(out[3]))
+
+    def set_linear_guard(self, max_cycles: int):
+        """bes_set_linear_guard: restart-cycle limit of one linear solve (0: default)."""
+        self._check(load().bes_set_linear_guard(self.h, int(max_cycles)))
+
+    def set_condition(self, cond: int, mach=None, U=None):
+        """bes_set_condition: a new condition (Mach vector, state or freestream) in slot cond."""
+        m = None if mach is None else np.ascontiguousarray(mach, dtype=np.float64)
+        u = None if U is None else np.ascontiguousarray(U, dtype=np.float64)
+        self._check(load().bes_set_condition(self.h, int(cond), None if m is None else _d(m),
+                                             None if u is None else _d(u)))
 
     def ilu_order(self) -> np.ndarray:
         o = np.zeros(self.n_cells, np.int64)

@@ -144,11 +144,28 @@ int bes_explicit_iterations(bes_ctx* ctx, int64_t n, double* history);
  * reads the matrix and the factors from 16-bit block-scaled copies and keeps the Krylov basis
  * in FP16), the update, and the
  * CFL control (adaptive as adaptCourantNum_, src/SolverImplicit.cpp:530-550, or the additive
- * geometric ramp).  history (may be NULL): [n][19] = L2[5] and max[5] of the Dt/V-scaled
+ * geometric ramp).  One step of every active condition is one CUDA graph launch: the GMRES
+ * iteration (Arnoldi steps, Givens rotations, restarts, convergence test) runs on the device
+ * inside the graph's conditional nodes, and the host synchronises once per step.
+ * history (may be NULL): [n][19] = L2[5] and max[5] of the Dt/V-scaled
  * right-hand side (the max is what the reference logs, Q10), CFL used, CFL after the step,
  * linear iterations, final relative linear residual, L2[5] of the unscaled residual
- * R = sum(+-F A) (the convergence measure). */
+ * R = sum(+-F A) (the convergence measure).  A frozen condition (bes_set_active) does not
+ * step; its history rows are zeros.  Returns BES_ERR_TIMEOUT when a linear solve was stopped
+ * by its restart-cycle limit (bes_set_linear_guard); the step is applied and the context stays
+ * usable. */
 int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history);
+
+/* Implicit-path statistics: out[0] steps taken, out[1] host synchronisations inside
+ * bes_implicit_steps (one per step), out[2] Arnoldi steps and out[3] restart cycles the device
+ * ran (each counted once per batched launch, whatever the number of conditions).  out [4]. */
+int bes_implicit_stats(const bes_ctx* ctx, int64_t* out);
+
+/* Limit of restart cycles per linear solve (0: linear_solver_max_iter + 1, more than a solve
+ * can take).  A solve that reaches the limit stops with its current iterate and the step
+ * returns BES_ERR_TIMEOUT.  The device loop over restart cycles ends by construction; this
+ * bound is its guard and lets a caller cap the work of one step. */
+int bes_set_linear_guard(bes_ctx* ctx, int32_t max_cycles);
 
 /* Assemble (without solving or updating) the implicit system at the current state and CFL
  * (SolverImplicit::computeFaceFluxes_ and the CoefficientMatrix, src/SolverImplicit.cpp:358-507).
@@ -157,12 +174,13 @@ int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history);
  * src/CoefficientMatrix.cpp:141-160).  Pass NULL arrays to query n_blocks. */
 int bes_implicit_assemble(bes_ctx* ctx, double cfl, double* rhs, double* blocks, int64_t* n_blocks);
 
-/* Event timing of the implicit path by kernel category (diagnostics for benchmarking).
- * enable 1 turns timing on (an event pair around every category's work, read back at the
- * step's synchronisation points), 0 off.  Returns (and resets) the accumulated milliseconds
- * and launch-group counts since the previous call: ms_out / counts_out [8] = residual (cell
- * sweep + face fluxes), Jacobians, assembly, ILU factorisation, preconditioner application,
- * matrix-vector products, Gram-Schmidt (dots, updates, normalisation), state update. */
+/* Device timing of the implicit path by kernel category (diagnostics for benchmarking).
+ * enable 1 turns timing on (the step graph then reads the GPU's nanosecond timer before and
+ * after every category's work inside the graph), 0 off.  Returns (and resets) the accumulated
+ * milliseconds and launch-group counts since the previous call: ms_out / counts_out [8] =
+ * residual (cell sweep + face fluxes), Jacobians, assembly, ILU factorisation, preconditioner
+ * application, matrix-vector products, Gram-Schmidt and GMRES control, state update.  A
+ * batched launch (all conditions of a batch) counts once. */
 int bes_profile(bes_ctx* ctx, int32_t enable, double* ms_out, int64_t* counts_out);
 
 /* The block-ILU(0) factorisation order (reference cell ids, colour by colour). */
@@ -215,12 +233,15 @@ int bes_wall_force(bes_ctx* ctx, double* force);  /* force [n_cond][3] */
  * per-condition array holds n_cond copies, every explicit kernel takes the condition from its
  * grid's y index, and one graph launch advances all conditions by one iteration.  State
  * arrays are [n_cond][n_cells][5], histories [n][n_cond][10] (explicit) or [n][n_cond][19]
- * (implicit), wall forces [n_cond][3].  The implicit solver steps the conditions one after
- * another through one set of implicit buffers (each condition keeps its own state, CFL
- * controller and freestream), so a batch needs the implicit memory of one condition only.
- * bes_compute_operators, bes_implicit_assemble and bes_solve need n_cond = 1; bes_write
- * writes condition 0; bes_sweep_run drives the explicit solver.  mach [n_cond][3] replaces
- * FREESTREAM_MACH. */
+ * (implicit), wall forces [n_cond][3].  The implicit solver advances all active conditions
+ * together (at most 256): each condition keeps its own state, CFL controller, freestream and
+ * Krylov side (basis, vectors, GMRES state, and with precision 2 its 16-bit matrix and factor
+ * copies); the residual, preconditioner, matrix-vector and Gram-Schmidt kernels take every
+ * condition in one launch, and the assembly and factorisation run condition by condition
+ * (with precision 2 through one shared FP32 scratch).  Each condition's result is bit for bit
+ * that of a context created for it alone.  bes_compute_operators, bes_implicit_assemble and
+ * bes_solve need n_cond = 1; bes_write writes condition 0; bes_sweep_run drives the explicit
+ * solver.  mach [n_cond][3] replaces FREESTREAM_MACH. */
 int bes_create_batch(const bes_mesh_arrays* mesh, const bes_options* opt, int32_t n_cond,
                      const double* mach, bes_ctx** out);
 int bes_conditions(const bes_ctx* ctx, int32_t* n_cond);
@@ -228,6 +249,13 @@ int bes_conditions(const bes_ctx* ctx, int32_t* n_cond);
 /* Freeze (0) or run (1) each condition, active [n_cond]: a frozen condition's kernels return
  * at once and its state is carried over unchanged. */
 int bes_set_active(bes_ctx* ctx, const int32_t* active);
+
+/* Replace condition `cond` of a context by a new one: freestream Mach vector mach [3] (NULL:
+ * keep the condition's), state U [n_cells][5] in reference numbering (NULL: the step-0
+ * freestream state); the condition is made active and, in an implicit context, its CFL
+ * control and step counters (CFL ramp, freestream ramp) restart at step 0.  Lets a sweep keep
+ * every slot of a batch busy: a converged condition's slot takes the next one. */
+int bes_set_condition(bes_ctx* ctx, int32_t cond, const double* mach, const double* U);
 
 /* Run every condition until its residual L2 (all five variables, relative to its first
  * iteration of this call) drops by `drop`, or max_iter iterations.  Convergence is checked

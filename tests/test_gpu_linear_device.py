@@ -1,0 +1,113 @@
+"""The implicit step as one graph launch: GMRES driven on the device, batched conditions.
+
+* One host synchronisation per implicit step, whatever the number of restart cycles: the
+  Arnoldi steps, Givens rotations, restarts and the convergence test run inside the step
+  graph's conditional nodes (bes_implicit_stats).
+* The device loop over restart cycles has a guard: a solve stopped by the restart-cycle limit
+  returns BES_ERR_TIMEOUT, its step is applied, and the context keeps working.
+* Frozen conditions of an implicit batch keep their state; a refilled slot
+  (bes_set_condition) gives bit for bit the run of a fresh context for its new condition.
+"""
+import numpy as np
+import pytest
+
+from bes_gb300 import build as nbuild
+from bes_gb300 import lib, meshgen
+
+pytestmark = pytest.mark.gpu
+
+MACHS = [(0.5, 0.0, 0.0), (0.7, 0.05, 0.0), meshgen.freestream_mach_vector(0.6, 3.0, -2.0)]
+IMPLICIT = dict(solver_type=1, local_time_step=1, courant_num=10.0,
+                adaptive_courant_num_max=500.0, linear_solver=1, linear_solver_tol=1e-2,
+                linear_solver_max_iter=200)
+
+
+def _opts(**kw):
+    base = dict(IMPLICIT)
+    base.update(kw)
+    return lib.default_options(**base)
+
+
+def _single(mesh, mach, n, **kw):
+    ctx = lib.Context(mesh, _opts(freestream_mach=mach, **kw))
+    h = ctx.implicit_steps(n)
+    U = ctx.get_state()
+    ctx.close()
+    return h, U
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_one_host_sync_per_implicit_step(precision):
+    nbuild.build()
+    mesh = meshgen.bump_channel(12, 4, 4, 0.08)
+    # GMRES(4) to 1e-6: several restart cycles per step
+    ctx = lib.Context(mesh, _opts(freestream_mach=MACHS[0], gmres_restart=4,
+                                  linear_solver_tol=1e-6, precision=precision))
+    h = ctx.implicit_steps(5)
+    s = ctx.implicit_stats()
+    ctx.close()
+    assert s["steps"] == 5
+    assert s["host_syncs"] == 5
+    assert s["arnoldi_steps"] == int(h[:, 12].sum())
+    assert s["restart_cycles"] >= int(np.ceil(h[:, 12] / 4).sum())
+    assert np.all(h[:, 13] <= 1e-6)
+
+
+def test_linear_guard_stops_a_solve_and_the_context_recovers():
+    nbuild.build()
+    mesh = meshgen.bump_channel(12, 4, 4, 0.08)
+    kw = dict(freestream_mach=MACHS[1], gmres_restart=2, linear_solver_tol=1e-8,
+              linear_solver_max_iter=400)
+    ctx = lib.Context(mesh, _opts(**kw))
+    ctx.set_linear_guard(1)
+    with pytest.raises(lib.BesError) as e:
+        ctx.implicit_steps(1)
+    assert e.value.code == 7  # BES_ERR_TIMEOUT
+    assert ctx.implicit_stats()["restart_cycles"] == 1
+    U1 = ctx.get_state()
+    assert np.all(np.isfinite(U1))
+    ctx.set_linear_guard(0)
+    h = ctx.implicit_steps(2)  # no limit but the iteration count: more than one cycle each
+    assert np.all(h[:, 12] > 2)
+    assert np.all(np.isfinite(ctx.get_state()))
+    ctx.close()
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_frozen_implicit_condition_keeps_its_state(precision):
+    nbuild.build()
+    mesh = meshgen.bump_channel(12, 4, 4, 0.08)
+    ctx = lib.Context(mesh, _opts(precision=precision), machs=MACHS)
+    ctx.implicit_steps(3)
+    U3 = ctx.get_state()
+    ctx.set_active([1, 0, 1])
+    h = ctx.implicit_steps(2)
+    U5 = ctx.get_state()
+    assert np.array_equal(U5[1], U3[1])
+    assert np.all(h[:, 1] == 0.0)
+    for b in (0, 2):
+        hs, Us = _single(mesh, MACHS[b], 5, precision=precision)
+        assert np.array_equal(U5[b], Us)
+        assert np.array_equal(h[:, b], hs[3:])
+    ctx.close()
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_refilled_slot_matches_a_fresh_context(precision):
+    nbuild.build()
+    mesh = meshgen.bump_channel(12, 4, 4, 0.08)
+    new_mach = meshgen.freestream_mach_vector(0.45, -2.0, 1.0)
+    ctx = lib.Context(mesh, _opts(precision=precision, cfl_ramp_steps=4, cfl_ramp_start=10.0,
+                                  cfl_ramp_end=200.0), machs=MACHS)
+    ctx.implicit_steps(3)
+    ctx.set_condition(1, mach=new_mach)
+    h = ctx.implicit_steps(4)
+    U = ctx.get_state()
+    kw = dict(precision=precision, cfl_ramp_steps=4, cfl_ramp_start=10.0, cfl_ramp_end=200.0)
+    hs, Us = _single(mesh, new_mach, 4, **kw)
+    assert np.array_equal(h[:, 1], hs)
+    assert np.array_equal(U[1], Us)
+    h0, U0 = _single(mesh, MACHS[0], 7, **kw)
+    assert np.array_equal(U[0], U0)
+    assert np.array_equal(h[:, 0], h0[3:])
+    ctx.close()

@@ -100,8 +100,9 @@ def test_sweep_run_stops_each_condition_at_its_drop():
 
 @pytest.mark.parametrize("precision", [0, 1, 2])
 def test_implicit_batch_matches_single_condition_runs(precision):
-    """Implicit batches step the conditions one after another through shared implicit
-    buffers; every condition, with its own adaptive CFL, matches its own context."""
+    """Implicit batches step all conditions together (batched Krylov kernels, per-condition
+    GMRES state on the device); every condition, with its own adaptive CFL, matches its own
+    context bit for bit."""
     nbuild.build()
     mesh = meshgen.bump_channel(12, 4, 4, 0.08)
     kw = dict(solver_type=1, courant_num=10.0, adaptive_courant_num_max=500.0,
