@@ -344,16 +344,17 @@ def explicit_fp64_work(nc: int, nf: int, cell_updates_per_s: float, n_stage: int
                     "cell sweep and the face flux are FP64-issue bound on this GPU"}
 
 
-def implicit_leg(args, torch, ctx, steps, warmup, flush, with_e2e):
+def implicit_leg(args, torch, ctx, steps, warmup, flush, with_e2e, prof_steps: int = 5):
     """warm-up, then `steps` timed implicit steps (events on the library stream around each
-    step, L2 flushed before each); returns timing, history and the kernel-category profile."""
-    nc = ctx.n_cells
+    step's graph launch, L2 flushed before each); then `prof_steps` more steps with the step
+    graph's device timer stamps on, for the kernel-category profile (the stamps are kernels of
+    their own, kept out of the timed steps).  Returns timing, history, state and profile."""
     ctx.implicit_steps(warmup)
     ext = torch.cuda.ExternalStream(ctx.stream_handle)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     c0 = ctx.counters()
-    ctx.profile(True)
+    s0 = ctx.implicit_stats()
     hist = []
     torch.cuda.synchronize()
     for k in range(steps):
@@ -363,12 +364,20 @@ def implicit_leg(args, torch, ctx, steps, warmup, flush, with_e2e):
         hist.append(ctx.implicit_steps(1)[0])
         ends[k].record(ext)
     torch.cuda.synchronize()
-    prof = ctx.profile(False)
     c1 = ctx.counters()
+    s1 = ctx.implicit_stats()
     dev_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
-    out = dict(ms=dev_ms, hist=np.array(hist), prof=prof,
+    out = dict(ms=dev_ms, hist=np.array(hist),
                launches=c1["launches"] - c0["launches"], state=ctx.get_state(),
-               force=ctx.wall_force())
+               force=ctx.wall_force(),
+               host_syncs_per_step=(s1["host_syncs"] - s0["host_syncs"]) / steps,
+               restart_cycles_per_step=(s1["restart_cycles"] - s0["restart_cycles"]) / steps)
+    if prof_steps > 0:
+        ctx.profile(True)
+        ph = ctx.implicit_steps(prof_steps)
+        out["prof"] = ctx.profile(False)
+        out["prof_steps"] = prof_steps
+        out["prof_linear_iterations"] = float(ph[..., 12].sum())
     if with_e2e:
         U = ctx.get_state()
         t0 = time.perf_counter()
@@ -435,7 +444,8 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
     o64 = dict(wl["opts"])
     o64["precision"] = 0
     ctx64 = lib.Context(mesh, lib.default_options(**o64))
-    plain = implicit_leg(args, torch, ctx64, args.steps, args.warmup, flush, with_e2e=False)
+    plain = implicit_leg(args, torch, ctx64, args.steps, args.warmup, flush, with_e2e=False,
+                         prof_steps=0)
     ctx64.close()
     prec = int(wl["opts"].get("precision", 0))
     prof = mixed["prof"]
@@ -471,12 +481,17 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
             "e2e": {"value": world * nc * args.steps / e2e_s, "unit": METRIC,
                     "h2d_bytes_per_step": 40 * nc, "d2h_bytes_per_step": 40 * nc},
             "gpu_launches": mixed["launches"],
+            "host_syncs_per_step": mixed["host_syncs_per_step"],
+            "restart_cycles_per_step": mixed["restart_cycles_per_step"],
             "roofline": {"kernel": KERNEL_NAMES[dom][prec],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": traffic_from_profiles(dom, args.workload, prec),
                          "ms_per_launch": per_launch_ms, "bytes_per_launch": cats[dom],
-                         "category_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()}},
+                         "timing": f"device timer stamps around each launch group inside the "
+                                   f"step graph, {mixed['prof_steps']} steps after the timed ones",
+                         "category_ms_per_step": {k: v[0] / mixed["prof_steps"]
+                                                  for k, v in prof.items()}},
             "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = implicit_cpu_baseline(wl)
