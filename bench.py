@@ -121,6 +121,32 @@ WORKLOADS = {
                                             linear_solver_max_iter=300, gmres_restart=30,
                                             cfl_ramp_steps=50, cfl_ramp_start=10.0,
                                             cfl_ramp_end=1000.0, precision=2)),
+    # converged batched sweep: 64 freestream conditions (numpy seed 0: Mach 0.3-0.85, pitch and
+    # sideslip -4..4 deg) on the 100x50x100-hex Gaussian-bump box (3.0M tets, stretching 1.05),
+    # each solved to a 1e-8 drop of its residual L2.  Production form: FP32 system with 16-bit
+    # block storage and FP64 residual/update, all conditions through the slots of one batched
+    # context (one graph launch per step of every slot, a converged slot takes the next
+    # condition), linear solves to prod_tol; plain form: the FP64 system, one condition per
+    # context, linear solves to 1e-2, on the first `plain_sample` conditions
+    "sweep_implicit_gauss_3m_64": dict(kind="isweep", mesh=("gauss", 100, 50, 100, 1.05),
+                                       conds=(0, 64), plain_sample=4, max_steps=400, slots=32,
+                                       prod_tol=0.1,
+                                       opts=dict(solver_type=1, local_time_step=1,
+                                                 courant_num=10.0, linear_solver=1,
+                                                 linear_solver_tol=1e-2,
+                                                 linear_solver_max_iter=300, gmres_restart=30,
+                                                 cfl_ramp_steps=50, cfl_ramp_start=10.0,
+                                                 cfl_ramp_end=1000.0, precision=2)),
+    # the same sweep at a validation size: 30x15x30-hex box (81,000 tets), 8 conditions
+    "sweep_implicit_gauss_81k_8": dict(kind="isweep", mesh=("gauss", 30, 15, 30, 1.05),
+                                       conds=(0, 8), plain_sample=2, max_steps=400, slots=4,
+                                       prod_tol=0.1,
+                                       opts=dict(solver_type=1, local_time_step=1,
+                                                 courant_num=10.0, linear_solver=1,
+                                                 linear_solver_tol=1e-2,
+                                                 linear_solver_max_iter=300, gmres_restart=30,
+                                                 cfl_ramp_steps=50, cfl_ramp_start=10.0,
+                                                 cfl_ramp_end=1000.0, precision=2)),
     # same scheme on the 200x60x30-hex channel (2.16M tets), Mach 0.84
     "explicit_bump_2m": dict(kind="explicit", mesh=("bump", 200, 60, 30, 0.08),
                              opts=dict(solver_type=0, local_time_step=1, courant_num=0.8,
@@ -705,6 +731,83 @@ def run_production(args, wl, torch, mesh, clocks):
             "clocks": clk}
 
 
+def run_isweep(args, wl, torch, mesh, clocks):
+    """Converged solves/hour of a batched implicit sweep against the plain FP64 solver.
+    value: cell-updates/s of the batched production sweep (cells x steps of every condition /
+    wall time of the whole sweep); converged_sweep: solves/hour of both forms, their ratio and
+    the force-coefficient differences on the conditions both solved."""
+    from bes_gb300 import lib, meshgen
+    seed, n = wl["conds"]
+    machs = np.array([meshgen.freestream_mach_vector(*c)
+                      for c in meshgen.sample_conditions(n, seed)])
+    nplain = min(n, wl["plain_sample"])
+    o64 = dict(wl["opts"], precision=0)
+    op = dict(wl["opts"], linear_solver_tol=wl["prod_tol"])
+    clocks.start()
+    # plain: the FP64 system, one condition per context, from the freestream
+    c64 = lib.Context(mesh, lib.default_options(**dict(o64, freestream_mach=tuple(machs[0]))))
+    nc = c64.n_cells
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p = c64.implicit_sweep(machs[:nplain], drop=1e-8, max_steps=wl["max_steps"])
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    c64.close()
+    # production: every condition through the slots of one batched context
+    slots = min(n, wl["slots"])
+    free, _ = torch.cuda.mem_get_info()
+    per_slot, shared = 1300.0 * nc, 3000.0 * nc  # bytes, with margin (implicit_allocate)
+    slots = max(1, min(slots, int((free - 8e9 - shared) // per_slot)))
+    cb = lib.Context(mesh, lib.default_options(**op), machs=machs[:slots])
+    used = free - torch.cuda.mem_get_info()[0]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s0 = cb.implicit_stats()
+    b = cb.implicit_sweep(machs, drop=1e-8, max_steps=wl["max_steps"])
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    s1 = cb.implicit_stats()
+    cb.close()
+    clk = clocks.stop()
+    conv_p = p["final_res"] <= 1e-8
+    conv_b = b["final_res"] <= 1e-8
+    sph_p = 3600.0 * conv_p.sum() / t_plain
+    sph_b = 3600.0 * conv_b.sum() / t_batch
+    rows = []
+    for q in range(nplain):
+        qd = 0.5 * float(np.sum(machs[q] ** 2))  # dynamic pressure (rho = 1, A_ref = 1)
+        rows.append(dict(mach=[float(x) for x in machs[q]],
+                         plain_steps=int(p["steps"][q]), plain_seconds=float(p["seconds"][q]),
+                         plain_converged=bool(conv_p[q]), batched_steps=int(b["steps"][q]),
+                         batched_converged=bool(conv_b[q]),
+                         force_coefficient_abs_diff=float(np.abs(b["force"][q] - p["force"][q]).max() / qd)))
+    both = [r for r in rows if r["plain_converged"] and r["batched_converged"]]
+    steps_b = int(b["steps"].sum())
+    return {"metric": METRIC, "metric_full": METRIC_FULL,
+            "value": nc * steps_b / t_batch, "unit": METRIC, "n_gpus": 1,
+            "steps": steps_b, "warmup": 0, "ms_per_step": t_batch / steps_b * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 system stored as fp16 blocks, fp16 Krylov basis / f64 residual and "
+                     "update", "data": "synthetic",
+            "config": {"workload": args.workload, "cells": nc, "conditions": n, "slots": slots,
+                       "device_bytes": int(used), "parallelism": "replicas1",
+                       "production_linear_tol": wl["prod_tol"],
+                       "l2": "not flushed (wall clock of whole solves)"},
+            "converged_sweep": {
+                "solves_per_hour": {"batched_fp32_system": sph_b, "plain_fp64": sph_p,
+                                    "ratio": sph_b / sph_p if sph_p else None},
+                "converged": {"batched_fp32_system": int(conv_b.sum()), "of": n,
+                              "plain_fp64": int(conv_p.sum()), "plain_of": nplain},
+                "seconds": {"batched_fp32_system": t_batch, "plain_fp64": t_plain},
+                "batched_steps_per_condition": [int(x) for x in b["steps"]],
+                "host_syncs": s1["host_syncs"] - s0["host_syncs"],
+                "max_force_coefficient_abs_diff": (max(r["force_coefficient_abs_diff"] for r in both)
+                                                   if both else None),
+                "target": "1e-8 x each condition's first residual L2 (both start from the "
+                          "freestream)"},
+            "per_condition_sampled": rows, "clocks": clk}
+
+
 def run_scale(args, wl, torch, mesh, clocks):
     """Batched implicit steps of many conditions on a large mesh: one step = one implicit step
     of every condition (stepped one after another through the shared implicit buffers); value =
@@ -814,9 +917,9 @@ def main():
     from bes_gb300 import lib
     nbuild.build()
     mesh = make_mesh(wl["mesh"])
-    if wl["kind"] in ("warmstart", "production", "scale"):
+    if wl["kind"] in ("warmstart", "production", "scale", "isweep"):
         fn = {"warmstart": run_warmstart, "production": run_production,
-              "scale": run_scale}[wl["kind"]]
+              "scale": run_scale, "isweep": run_isweep}[wl["kind"]]
         line = fn(args, wl, torch, mesh, ClockSampler(local_rank))
         if rank == 0:
             print(json.dumps(line))

@@ -29,7 +29,7 @@ EXPORTED = [
     "bes_ilu_order", "bes_counters", "bes_wall_force", "bes_profile",
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
     "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
-    "bes_implicit_stats", "bes_set_linear_guard", "bes_set_condition",
+    "bes_implicit_stats", "bes_set_linear_guard", "bes_set_condition", "bes_implicit_sweep",
     "bes_mlp_create", "bes_mlp_destroy", "bes_mlp_last_error", "bes_mlp_train", "bes_mlp_infer",
     "bes_mlp_init_state", "bes_mlp_params", "bes_mlp_features", "bes_mlp_loss_grad",
     "bes_mlp_apply_grad", "bes_mlp_normalisation",
@@ -141,6 +141,8 @@ def load(path: str = LIB_PATH):
     L.bes_implicit_stats.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_set_linear_guard.argtypes = [P, ctypes.c_int32]
     L.bes_set_condition.argtypes = [P, ctypes.c_int32, D, D]
+    L.bes_implicit_sweep.argtypes = [P, ctypes.c_int32, D, D, D, ctypes.c_double, ctypes.c_int64,
+                                     ctypes.POINTER(ctypes.c_int64), D, D, D, D]
     F32 = ctypes.POINTER(ctypes.c_float)
     I64p = ctypes.POINTER(ctypes.c_int64)
     L.bes_mlp_create.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(P)]
@@ -479,6 +481,28 @@ class Context:
         u = None if U is None else np.ascontiguousarray(U, dtype=np.float64)
         self._check(load().bes_set_condition(self.h, int(cond), None if m is None else _d(m),
                                              None if u is None else _d(u)))
+
+    def implicit_sweep(self, machs, drop: float = 1e-8, max_steps: int = 300, U0=None,
+                       target=None, states: bool = False) -> dict:
+        """bes_implicit_sweep: solve every condition of `machs` [n, 3] to convergence through
+        the context's slots; returns per-condition steps, final relative residual, wall force,
+        seconds (and final states when `states`)."""
+        m = np.ascontiguousarray(machs, dtype=np.float64).reshape(-1, 3)
+        n = m.shape[0]
+        u0 = None if U0 is None else np.ascontiguousarray(U0, dtype=np.float64)
+        tg = None if target is None else np.ascontiguousarray(target, dtype=np.float64)
+        steps = np.zeros(n, np.int64)
+        fin = np.zeros(n)
+        force = np.zeros((n, 3))
+        secs = np.zeros(n)
+        U = np.zeros((n, self.n_cells, 5)) if states else None
+        self._check(load().bes_implicit_sweep(self.h, n, _d(m), _d(u0), _d(tg), float(drop),
+                                              int(max_steps), _i(steps), _d(fin), _d(force),
+                                              _d(U), _d(secs)))
+        out = dict(steps=steps, final_res=fin, force=force, seconds=secs)
+        if states:
+            out["U"] = U
+        return out
 
     def ilu_order(self) -> np.ndarray:
         o = np.zeros(self.n_cells, np.int64)

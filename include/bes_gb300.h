@@ -257,6 +257,22 @@ int bes_set_active(bes_ctx* ctx, const int32_t* active);
  * every slot of a batch busy: a converged condition's slot takes the next one. */
 int bes_set_condition(bes_ctx* ctx, int32_t cond, const double* mach, const double* U);
 
+/* Solve n conditions to convergence with the implicit solver, through the context's slots (a
+ * batched implicit context): each slot takes a condition of the queue (bes_set_condition with
+ * mach [n][3] and, if U0 is not NULL, the initial state U0 [n][n_cells][5] in reference
+ * numbering, e.g. a learned warm start; else the freestream), all slots step together, and a
+ * slot whose condition is finished takes the next one.  A condition is finished when its
+ * residual L2 (R = sum(+-F A), all five variables) is <= target[q] (if target is not NULL and
+ * target[q] > 0), else <= drop times its first step's residual; or when it is not finite; or
+ * after max_steps steps.  Per condition (each output may be NULL): steps [n], final_res [n]
+ * its last residual relative to its first, force [n][3] the slip-wall pressure force of its
+ * final state (bes_wall_force), U_out [n][n_cells][5] its final state, seconds [n] wall time
+ * from its start to its finish.  No counterpart in the reference, which solves one condition
+ * per process (src/BES.cpp:94-111). */
+int bes_implicit_sweep(bes_ctx* ctx, int32_t n, const double* mach, const double* U0,
+                       const double* target, double drop, int64_t max_steps, int64_t* steps,
+                       double* final_res, double* force, double* U_out, double* seconds);
+
 /* Run every condition until its residual L2 (all five variables, relative to its first
  * iteration of this call) drops by `drop`, or max_iter iterations.  Convergence is checked
  * every check_every iterations; converged conditions are frozen from then on.  iters [n_cond]

@@ -111,3 +111,39 @@ def test_refilled_slot_matches_a_fresh_context(precision):
     assert np.array_equal(U[0], U0)
     assert np.array_equal(h[:, 0], h0[3:])
     ctx.close()
+
+
+def _single_to_drop(mesh, mach, drop, max_steps, **kw):
+    ctx = lib.Context(mesh, _opts(freestream_mach=mach, **kw))
+    r0 = None
+    for k in range(max_steps):
+        h = ctx.implicit_steps(1)[0]
+        r = float(np.sqrt(np.sum(h[14:19] ** 2)))
+        r0 = r if r0 is None else r0
+        if r <= drop * r0:
+            break
+    out = (k + 1, r / r0, ctx.get_state(), ctx.wall_force())
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_sweep_queue_through_slots_matches_single_solves(precision):
+    """Five conditions through two slots (bes_implicit_sweep): each gives the steps, final
+    residual, state and wall force of its own single-condition solve, bit for bit."""
+    nbuild.build()
+    mesh = meshgen.bump_channel(12, 4, 4, 0.08)
+    machs = np.array([meshgen.freestream_mach_vector(m, a, b)
+                      for m, a, b in [(0.5, 0, 0), (0.6, 2, -1), (0.45, -3, 2), (0.7, 1, 1),
+                                      (0.55, 0, 3)]])
+    kw = dict(precision=precision, adaptive_courant_num_max=1000.0)
+    ctx = lib.Context(mesh, _opts(**kw), machs=machs[:2])
+    out = ctx.implicit_sweep(machs, drop=1e-6, max_steps=150, states=True)
+    ctx.close()
+    for q, m in enumerate(machs):
+        steps, fin, U, F = _single_to_drop(mesh, m, 1e-6, 150, **kw)
+        assert out["steps"][q] == steps < 150
+        assert out["final_res"][q] == pytest.approx(fin, rel=1e-14)
+        assert np.array_equal(out["U"][q], U)
+        assert np.array_equal(out["force"][q], F)
+        assert out["seconds"][q] > 0
