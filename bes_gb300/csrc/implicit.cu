@@ -270,7 +270,8 @@ template <class T, class B>
 void enqueue_arnoldi(const Sys<T, B>& S, cudaStream_t s, int j, const GmresParam& P,
                      const GmresHandles& h) {
   bes_ctx* c = S.c;
-  const int32_t* cyc = c->imp.gm.cyc;
+  // with one slot the IF node alone decides whether the step runs: no per-block flag load
+  const int32_t* cyc = S.nslot > 1 ? c->imp.gm.cyc : nullptr;
   const int nv = j + 1;
   stamp(c, s, PROF_PRECOND, 1);
   enqueue_precond(S, s, S.precond_in(j), cyc);
@@ -304,23 +305,25 @@ void enqueue_cycle_end(const Sys<T, B>& S, cudaStream_t s, const GmresParam& P,
                        const GmresHandles& h) {
   bes_ctx* c = S.c;
   const GmresDev& g = c->imp.gm;
+  // with one slot the WHILE node alone decides whether the cycle end runs
+  const int32_t* lin = S.nslot > 1 ? g.lin : nullptr;
   stamp(c, s, PROF_ORTHO, 1);
   gmres_solve_y_kernel<<<1, S.nthr, 0, s>>>(g, S.nslot);
   lincomb_kernel<T, B><<<S.vgrid, 256, 0, s>>>(S.vec(S.W), S.cbasis(0), S.ldv, g.jc,
                                                cslots((const double*)g.y, (int64_t)kMaxRestart),
-                                               S.N, g.lin);
+                                               S.N, lin);
   stamp(c, s, PROF_ORTHO, 0);
   stamp(c, s, PROF_PRECOND, 1);
-  enqueue_precond(S, s, S.cvec(S.W), g.lin);
+  enqueue_precond(S, s, S.cvec(S.W), lin);
   stamp(c, s, PROF_PRECOND, 0);
   stamp(c, s, PROF_SPMV, 1);
-  add_kernel<T><<<S.vgrid, 256, 0, s>>>(S.vec(S.X), S.cvec(S.Z), S.N, g.lin);
-  enqueue_spmv(S, s, S.cvec(S.X), S.cvec(S.b), S.vec(S.W), g.lin);
+  add_kernel<T><<<S.vgrid, 256, 0, s>>>(S.vec(S.X), S.cvec(S.Z), S.N, lin);
+  enqueue_spmv(S, s, S.cvec(S.X), S.cvec(S.b), S.vec(S.W), lin);
   stamp(c, s, PROF_SPMV, 0);
   stamp(c, s, PROF_ORTHO, 1);
-  norm2_kernel<T><<<S.vgrid, 256, 0, s>>>(S.cvec(S.W), S.N, S.red(), g.lin);
+  norm2_kernel<T><<<S.vgrid, 256, 0, s>>>(S.cvec(S.W), S.N, S.red(), lin);
   reduce_slots_kernel<<<dim3(1, S.nslot), 256, 0, s>>>(S.cred(), kRedBlocks, 1, 0, S.dev(kGsR),
-                                                       g.lin);
+                                                       lin);
   gmres_restart_kernel<<<1, S.nthr, 0, s>>>(g, P, h, S.nslot, c->imp.guard_dev);
   basis_start_kernel<T, B><<<S.vgrid, 256, 0, s>>>(S.basis(0), S.vec(S.Vx), S.cvec(S.W),
                                                    cslots((const double*)g.sc, 8LL), S.N, g.cyc);

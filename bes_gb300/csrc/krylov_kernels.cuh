@@ -48,16 +48,10 @@ __device__ __forceinline__ bool slot_idle(const int32_t* run) {
 //   UPPER only        colours C-2..0 of the backward sweep: out_i = inv(U_ii)(y_i - sum U_ik z_k)
 // `in` and `out` must not alias.
 template <class T, bool LOWER, bool UPPER>
-__global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int r1, int s1,
-                                                         SlotPtr<const T> Ap, SlotPtr<const T> Dp,
-                                                         SlotPtr<const T> inp, SlotPtr<T> outp,
-                                                         const int32_t* run) {
-  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= r1 || slot_idle(run)) return;
-  const T* __restrict__ A = Ap.at();
-  const T* __restrict__ Dinv = Dp.at();
-  const T* __restrict__ in = inp.at();
-  T* __restrict__ out = outp.at();
+__device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, int r1, int s1,
+                                               const T* __restrict__ A,
+                                               const T* __restrict__ Dinv,
+                                               const T* __restrict__ in, T* __restrict__ out) {
   const int nc = m.nc;
   const T* own = (LOWER || r0 == 0) ? in : out;
   T acc[5];
@@ -92,19 +86,23 @@ __global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int 
   }
 }
 
-// ilu_colour_kernel with packed factors: L / U blocks in H slots 0..3 (local faces 0..3),
-// inv(U_ii) in D (one slot)
-template <bool LOWER, bool UPPER>
-__global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
-    DevMesh m, int r0, int r1, int s1, SlotPtr<const __half2> Hp, SlotPtr<const float> HSp,
-    SlotPtr<const __half2> Dp, SlotPtr<const float> DSp, SlotPtr<const float> inp,
-    SlotPtr<float> outp, const int32_t* run) {
+// (at least 16 blocks of 128 threads per SM: the slot offsets would otherwise take the
+// registers of a quarter of the resident blocks)
+template <class T, bool LOWER, bool UPPER>
+__global__ void __launch_bounds__(128, 16) ilu_colour_kernel(DevMesh m, int r0, int r1, int s1,
+                                                         SlotPtr<const T> Ap, SlotPtr<const T> Dp,
+                                                         SlotPtr<const T> inp, SlotPtr<T> outp,
+                                                         const int32_t* run) {
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1 || slot_idle(run)) return;
-  const __half2* __restrict__ H = Hp.at();
-  const float* __restrict__ HS = HSp.at();
-  const float* __restrict__ in = inp.at();
-  float* __restrict__ out = outp.at();
+  ilu_colour_row<T, LOWER, UPPER>(m, i, r0, r1, s1, Ap.at(), Dp.at(), inp.at(), outp.at());
+}
+
+template <bool LOWER, bool UPPER>
+__device__ __forceinline__ void ilu_colour_packed_row(
+    const DevMesh& m, int i, int r0, int r1, int s1, const __half2* __restrict__ H,
+    const float* __restrict__ HS, const __half2* __restrict__ D, const float* __restrict__ DS,
+    const float* __restrict__ in, float* __restrict__ out) {
   const int nc = m.nc;
   const float* own = (LOWER || r0 == 0) ? in : out;
   float acc[5];
@@ -133,8 +131,8 @@ __global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
   }
   if (UPPER) {
     float a[26];
-    load_packed(Dp.at(), 0, nc, i, a);
-    const float sc = DSp.at()[i];
+    load_packed(D, 0, nc, i, a);
+    const float sc = DS[i];
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       float x = 0.0f;
@@ -146,6 +144,19 @@ __global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[(int64_t)i * 5 + v] = acc[v];
   }
+}
+
+// ilu_colour_kernel with packed factors: L / U blocks in H slots 0..3 (local faces 0..3),
+// inv(U_ii) in D (one slot)
+template <bool LOWER, bool UPPER>
+__global__ void __launch_bounds__(128, 16) ilu_colour_packed_kernel(
+    DevMesh m, int r0, int r1, int s1, SlotPtr<const __half2> Hp, SlotPtr<const float> HSp,
+    SlotPtr<const __half2> Dp, SlotPtr<const float> DSp, SlotPtr<const float> inp,
+    SlotPtr<float> outp, const int32_t* run) {
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1 || slot_idle(run)) return;
+  ilu_colour_packed_row<LOWER, UPPER>(m, i, r0, r1, s1, Hp.at(), HSp.at(), Dp.at(), DSp.at(),
+                                      inp.at(), outp.at());
 }
 
 // Level-scheduled block ILU(0) in reverse Cuthill-McKee order: forward solve of one stage,

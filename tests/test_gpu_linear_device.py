@@ -130,19 +130,22 @@ def _single_to_drop(mesh, mach, drop, max_steps, **kw):
 @pytest.mark.parametrize("precision", [0, 2])
 def test_sweep_queue_through_slots_matches_single_solves(precision):
     """Five conditions through two slots (bes_implicit_sweep): each gives the steps, final
-    residual, state and wall force of its own single-condition solve, bit for bit."""
+    residual, state and wall force of its own single-condition solve, bit for bit.  On this
+    4 % bump the oracle's FP64 solve reaches a 1e-6 drop in about 65 steps at Mach 0.45, 0.5,
+    0.6 and 0.65 and stalls near 1e-3 at Mach 0.55, which ends at the step limit."""
     nbuild.build()
-    mesh = meshgen.bump_channel(12, 4, 4, 0.08)
-    machs = np.array([meshgen.freestream_mach_vector(m, a, b)
-                      for m, a, b in [(0.5, 0, 0), (0.6, 2, -1), (0.45, -3, 2), (0.7, 1, 1),
-                                      (0.55, 0, 3)]])
-    kw = dict(precision=precision, adaptive_courant_num_max=1000.0)
+    mesh = meshgen.bump_channel(24, 8, 6, 0.04)
+    machs = np.array([(m, 0.0, 0.0) for m in (0.5, 0.55, 0.45, 0.6, 0.65)])
+    kw = dict(precision=precision, cfl_ramp_steps=10, cfl_ramp_start=10.0, cfl_ramp_end=1000.0)
     ctx = lib.Context(mesh, _opts(**kw), machs=machs[:2])
-    out = ctx.implicit_sweep(machs, drop=1e-6, max_steps=150, states=True)
+    out = ctx.implicit_sweep(machs, drop=1e-6, max_steps=100, states=True)
     ctx.close()
+    assert out["steps"][1] == 100 and out["final_res"][1] > 1e-6
     for q, m in enumerate(machs):
-        steps, fin, U, F = _single_to_drop(mesh, m, 1e-6, 150, **kw)
-        assert out["steps"][q] == steps < 150
+        steps, fin, U, F = _single_to_drop(mesh, m, 1e-6, 100, **kw)
+        assert out["steps"][q] == steps
+        if q != 1:
+            assert steps < 100 and fin <= 1e-6
         assert out["final_res"][q] == pytest.approx(fin, rel=1e-14)
         assert np.array_equal(out["U"][q], U)
         assert np.array_equal(out["force"][q], F)
