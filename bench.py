@@ -129,7 +129,7 @@ WORKLOADS = {
     # condition), linear solves to prod_tol; plain form: the FP64 system, one condition per
     # context, linear solves to 1e-2, on the first `plain_sample` conditions
     "sweep_implicit_gauss_3m_64": dict(kind="isweep", mesh=("gauss", 100, 50, 100, 1.05),
-                                       conds=(0, 64), plain_sample=4, max_steps=400, slots=32,
+                                       conds=(0, 64), plain_sample=4, max_steps=300, slots=32,
                                        prod_tol=0.1,
                                        opts=dict(solver_type=1, local_time_step=1,
                                                  courant_num=10.0, linear_solver=1,

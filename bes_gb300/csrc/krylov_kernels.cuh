@@ -86,10 +86,8 @@ __device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, 
   }
 }
 
-// (at least 16 blocks of 128 threads per SM: the slot offsets would otherwise take the
-// registers of a quarter of the resident blocks)
 template <class T, bool LOWER, bool UPPER>
-__global__ void __launch_bounds__(128, 16) ilu_colour_kernel(DevMesh m, int r0, int r1, int s1,
+__global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int r1, int s1,
                                                          SlotPtr<const T> Ap, SlotPtr<const T> Dp,
                                                          SlotPtr<const T> inp, SlotPtr<T> outp,
                                                          const int32_t* run) {
@@ -149,7 +147,7 @@ __device__ __forceinline__ void ilu_colour_packed_row(
 // ilu_colour_kernel with packed factors: L / U blocks in H slots 0..3 (local faces 0..3),
 // inv(U_ii) in D (one slot)
 template <bool LOWER, bool UPPER>
-__global__ void __launch_bounds__(128, 16) ilu_colour_packed_kernel(
+__global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
     DevMesh m, int r0, int r1, int s1, SlotPtr<const __half2> Hp, SlotPtr<const float> HSp,
     SlotPtr<const __half2> Dp, SlotPtr<const float> DSp, SlotPtr<const float> inp,
     SlotPtr<float> outp, const int32_t* run) {
