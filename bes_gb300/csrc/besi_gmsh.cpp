@@ -206,6 +206,10 @@ extern "C" int bes_options_from_besi(const char* path, bes_options* o, char* mes
       o->cfl_ramp_steps = (int32_t)x;
       o->cfl_ramp_start = a;
       o->cfl_ramp_end = b;
+    } else if (key == "SWEEP_KERNEL") {  // additive
+      const int w = word({"AUTO", "PER_COLOUR", "PERSISTENT"});
+      if (w < 0) return bad("SWEEP_KERNEL must be AUTO, PER_COLOUR or PERSISTENT");
+      o->sweep_kernel = w;
     } else if (key == "JACOBIAN_REPEAT") {  // additive: 5 reproduces the reference
       if (!num(0, x) || x < 1) return bad("JACOBIAN_REPEAT must be >= 1");
       o->jacobian_repeat = (int32_t)x;

@@ -161,6 +161,16 @@ struct ImplicitBuffers {
   int32_t* stage_rows = nullptr;  // block-ILU(0) rows grouped by stage
   int32_t* ilu_pos = nullptr;     // factorisation position of each cell
   bool use_colour_ranges = false;          // colour order on contiguous colour ranges
+  // colour sweeps: one launch per colour, or one persistent launch per sweep (grid of
+  // resident blocks with a bounded grid barrier between colours); chosen by the autotuner on
+  // the first step unless the options fix it
+  int sweep_kernel = 1;        // 1 per colour, 2 persistent
+  bool tuned = false;
+  int persistent_blocks = 0;   // grid of the persistent sweep
+  unsigned int* sync_count = nullptr;  // grid barrier: arrivals, generation, error flag
+  unsigned int* sync_gen = nullptr;
+  int* sync_error = nullptr;
+  std::string tuning;          // the autotuner's report
   // one graph per implicit step: [profiled][snapshot], built on first use; kernel nodes of its
   // sections (top level, one slot's assembly, one Arnoldi step, one restart-cycle end)
   cudaGraphExec_t step_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};

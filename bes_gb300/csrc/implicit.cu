@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdio>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -177,6 +178,66 @@ int end_conditional(bes_ctx* c, cudaStream_t child, int64_t* kernels) {
 
 // ---- Krylov side, batched over slots -----------------------------------------------------
 
+// The colour stages of a sweep: colours 1..C-2 forward, the last colour's two solves fused,
+// colours C-2..0 backward.  False if there are more stages than a persistent sweep holds.
+bool sweep_plan(const SoaMesh& M, SweepPlan& P) {
+  const int C = M.n_stages;
+  if (C < 1 || 2 * C - 1 > kMaxStages) return false;
+  P = SweepPlan();
+  P.s1 = C > 1 ? M.stage_off[1] : M.stage_off[C];
+  auto add = [&](int k, int kind) {
+    P.r0[P.n] = M.stage_off[k];
+    P.r1[P.n] = M.stage_off[k + 1];
+    P.kind[P.n] = kind;
+    ++P.n;
+  };
+  for (int k = 1; k < C - 1; ++k) add(k, 0);
+  add(C - 1, 1);
+  for (int k = C - 2; k >= 0; --k) add(k, 2);
+  return true;
+}
+
+// One persistent launch of the whole colour sweep from `in` into Z (cooperative: every block
+// of the grid is resident, which the grid barrier between colours needs).
+template <class T, class B>
+cudaError_t launch_persistent_sweep(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> in,
+                                    const int32_t* run) {
+  bes_ctx* c = S.c;
+  const ImplicitBuffers& I = c->imp;
+  SweepPlan P;
+  if (!sweep_plan(c->soa, P)) return cudaErrorInvalidConfiguration;
+  SweepOps<T> O;
+  std::memset(&O, 0, sizeof(O));
+  if (S.packed) {
+    O.H = cslots((const __half2*)S.LU16, 52LL * S.nc);
+    O.HS = cslots((const float*)S.LUs, 4LL * S.nc);
+    O.D = cslots((const __half2*)S.D16, 13LL * S.nc);
+    O.DS = cslots((const float*)S.Ds, (int64_t)S.nc);
+  } else {
+    O.L = cslots((const T*)S.LU, S.sA);
+    O.Dinv = cslots((const T*)S.Dinv, S.sDinv);
+  }
+  O.in = in;
+  O.out = S.vec(S.Z);
+  const GridSync gs{I.sync_count, I.sync_gen, I.sync_error};
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(I.persistent_blocks);
+  cfg.blockDim = dim3(128);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if constexpr (std::is_same<T, float>::value)
+    if (S.packed)
+      return cudaLaunchKernelEx(&cfg, ilu_sweep_persistent_kernel<float, true>, c->dm, P, O,
+                                S.nslot, run, gs);
+  return cudaLaunchKernelEx(&cfg, ilu_sweep_persistent_kernel<T, false>, c->dm, P, O, S.nslot,
+                            run, gs);
+}
+
 // Z = M^{-1} in for every slot whose run flag is set
 template <class T, class B>
 void enqueue_precond(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> in, const int32_t* run) {
@@ -184,6 +245,10 @@ void enqueue_precond(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> in, co
   const SoaMesh& M = c->soa;
   const DevMesh& m = c->dm;
   SlotPtr<T> Z = S.vec(S.Z);
+  if (uses_ilu(c) && c->imp.use_colour_ranges && c->imp.sweep_kernel == 2) {
+    launch_persistent_sweep(S, s, in, run);
+    return;
+  }
   if (!uses_ilu(c)) {
     if constexpr (std::is_same<T, float>::value) {
       if (S.packed) {
@@ -445,6 +510,106 @@ void enqueue_factor(const Sys<T, B>& S, cudaStream_t s, int k) {
   stamp(c, s, PROF_ILU_FACTOR, 0);
 }
 
+// ---- autotuner ------------------------------------------------------------------------------
+
+int reset_grid_sync(bes_ctx* c) {
+  ImplicitBuffers& I = c->imp;
+  IMP_TRY(c, cudaMemsetAsync(I.sync_count, 0, sizeof(unsigned), c->stream));
+  IMP_TRY(c, cudaMemsetAsync(I.sync_gen, 0, sizeof(unsigned), c->stream));
+  IMP_TRY(c, cudaMemsetAsync(I.sync_error, 0, sizeof(int), c->stream));
+  IMP_TRY(c, cudaStreamSynchronize(c->stream));
+  return BES_OK;
+}
+
+// The colour-sweep variant, timed on this context's mesh and slots: one launch per colour, or
+// one persistent launch per sweep.  Each candidate runs 3 untimed and 10 timed sweeps (CUDA
+// events on the context's stream, all slots); a persistent candidate whose launch fails or
+// whose grid barrier gives up is dropped.  The options can fix the variant instead.
+template <class T, class B>
+int tune_sweep(bes_ctx* c) {
+  ImplicitBuffers& I = c->imp;
+  Sys<T, B> S(c);
+  I.tuned = true;
+  char line[256];
+  if (!uses_ilu(c) || !I.use_colour_ranges) {
+    I.sweep_kernel = 1;
+    return BES_OK;
+  }
+  SweepPlan plan;
+  const bool can_persist = sweep_plan(c->soa, plan) && I.persistent_blocks > 0;
+  if (c->opt.sweep_kernel == 1 || c->opt.sweep_kernel == 2) {
+    I.sweep_kernel = (c->opt.sweep_kernel == 2 && can_persist) ? 2 : 1;
+    std::snprintf(line, sizeof(line), "colour sweep: %s (fixed by the options)\n",
+                  I.sweep_kernel == 2 ? "persistent" : "one launch per colour");
+    I.tuning += line;
+    return BES_OK;
+  }
+  cudaEvent_t e0, e1;
+  IMP_TRY(c, cudaEventCreate(&e0));
+  IMP_TRY(c, cudaEventCreate(&e1));
+  double best = 1e300;
+  int choice = 1;
+  std::string rep = "colour sweep:";
+  for (int cand = 1; cand <= 2; ++cand) {
+    if (cand == 2 && !can_persist) {
+      rep += " persistent not possible;";
+      continue;
+    }
+    I.sweep_kernel = cand;
+    bool ok = true;
+    float ms = 0.0f;
+    for (int r = 0; r < 13 && ok; ++r) {
+      if (r == 3) cudaEventRecord(e0, c->stream);
+      if (cand == 2)
+        ok = launch_persistent_sweep(S, c->stream, S.cvec(S.b), nullptr) == cudaSuccess;
+      else
+        enqueue_precond(S, c->stream, S.cvec(S.b), nullptr);
+    }
+    cudaEventRecord(e1, c->stream);
+    const cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      c->last_error = std::string("colour-sweep tuning: ") + cudaGetErrorString(e);
+      return BES_ERR_CUDA;
+    }
+    if (ok) {
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (cand == 2) {
+        int err = 0;
+        cudaMemcpy(&err, I.sync_error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (err) ok = false;
+      }
+    }
+    cudaGetLastError();  // a refused cooperative launch leaves no sticky error
+    if (cand == 2) {
+      const int rc = reset_grid_sync(c);
+      if (rc) return rc;
+    }
+    const double per = ms / 10.0;
+    if (cand == 1)
+      std::snprintf(line, sizeof(line), " one launch per colour %.4f ms;", per);
+    else if (ok)
+      std::snprintf(line, sizeof(line), " persistent (%d blocks of 128) %.4f ms;",
+                    I.persistent_blocks, per);
+    else
+      std::snprintf(line, sizeof(line), " persistent failed;");
+    rep += line;
+    if (ok && per < best) {
+      best = per;
+      choice = cand;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  I.sweep_kernel = choice;
+  std::snprintf(line, sizeof(line), " taken: %s (%d slots, %d cells)\n",
+                choice == 2 ? "persistent" : "one launch per colour", S.nslot, S.nc);
+  rep += line;
+  I.tuning += rep;
+  return BES_OK;
+}
+
 // ---- the step graph -------------------------------------------------------------------------
 
 // Device address of slot k's norms in the device array of step results.
@@ -522,9 +687,21 @@ int build_step_graph(bes_ctx* c, int prof) {
     IMP_TRY(c, cudaStreamCreateWithFlags(&I.cap[0], cudaStreamNonBlocking));
     IMP_TRY(c, cudaStreamCreateWithFlags(&I.cap[1], cudaStreamNonBlocking));
   }
+  if (!I.tuned) {
+    const int rc = tune_sweep<T, B>(c);
+    if (rc) return rc;
+  }
   cudaGraph_t g = nullptr;
   t_stamps = prof != 0;
-  const int rc = capture_step<T, B>(c, prof, &g);
+  int rc = capture_step<T, B>(c, prof, &g);
+  if (rc && I.sweep_kernel == 2) {
+    // the persistent launch could not be captured: one launch per colour
+    abandon_capture(c);
+    I.sweep_kernel = 1;
+    I.tuning += "colour sweep: the persistent launch could not be captured in the step graph; "
+                "taken: one launch per colour\n";
+    rc = capture_step<T, B>(c, prof, &g);
+  }
   t_stamps = false;
   if (rc) {
     abandon_capture(c);
@@ -605,14 +782,22 @@ int run_steps(bes_ctx* c, int64_t n, double* history) {
     int rc = upload_step_inputs(c, act, cfl, P);
     if (rc) return rc;
     IMP_TRY(c, cudaGraphLaunch(I.step_graph[prof][c->cur], c->stream));
-    int nan = 0;
+    int nan = 0, sync_err = 0;
     unsigned long long cnt[2];
     IMP_TRY(c, cudaMemcpyAsync(I.res_host.data(), I.res, ns * sizeof(StepResult),
                                cudaMemcpyDeviceToHost, c->stream));
     IMP_TRY(c, cudaMemcpyAsync(cnt, I.gm.counters, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     IMP_TRY(c, cudaMemcpyAsync(&nan, c->nan_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    IMP_TRY(c, cudaMemcpyAsync(&sync_err, I.sync_error, sizeof(int), cudaMemcpyDeviceToHost,
+                               c->stream));
     IMP_TRY(c, cudaStreamSynchronize(c->stream));
     ++I.host_syncs;
+    if (sync_err) {
+      if ((rc = reset_grid_sync(c))) return rc;
+      c->last_error = "a grid barrier of the persistent colour sweep gave up after one second; "
+                      "the step's linear solves are not valid";
+      return BES_ERR_TIMEOUT;
+    }
     // kernels this step launched: the graph's top level, the assembly of each slot that
     // stepped, and the Arnoldi and restart-cycle bodies the device ran
     int nact = 0;
@@ -828,6 +1013,9 @@ int implicit_allocate(bes_ctx* c) {
   rc |= imp_malloc(c, (void**)&I.act, ns * sizeof(int32_t));
   rc |= imp_malloc(c, (void**)&I.guard_dev, sizeof(int32_t));
   rc |= imp_malloc(c, (void**)&c->prof.dev, 3 * PROF_NCAT * sizeof(unsigned long long));
+  rc |= imp_malloc(c, (void**)&I.sync_count, sizeof(unsigned));
+  rc |= imp_malloc(c, (void**)&I.sync_gen, sizeof(unsigned));
+  rc |= imp_malloc(c, (void**)&I.sync_error, sizeof(int));
   rc |= imp_malloc(c, (void**)&I.m_own, nf);
   rc |= imp_malloc(c, (void**)&I.m_nb, nf);
   rc |= imp_malloc(c, (void**)&I.stage_rows, nc * sizeof(int32_t));
@@ -838,6 +1026,25 @@ int implicit_allocate(bes_ctx* c) {
   IMP_TRY(c, cudaMemset(g.cyc, 0, ns * sizeof(int32_t)));
   IMP_TRY(c, cudaMemset(g.counters, 0, 2 * sizeof(unsigned long long)));
   IMP_TRY(c, cudaMemset(I.guard_dev, 0, sizeof(int32_t)));
+  IMP_TRY(c, cudaMemset(I.sync_count, 0, sizeof(unsigned)));
+  IMP_TRY(c, cudaMemset(I.sync_gen, 0, sizeof(unsigned)));
+  IMP_TRY(c, cudaMemset(I.sync_error, 0, sizeof(int)));
+  {
+    // persistent colour sweep: every block resident (occupancy x SMs), if the device can
+    // launch cooperatively
+    int coop = 0, sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    cudaError_t e;
+    if (I.packed)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ilu_sweep_persistent_kernel<float, true>, 128, 0);
+    else if (I.prec)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ilu_sweep_persistent_kernel<float, false>, 128, 0);
+    else
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ilu_sweep_persistent_kernel<double, false>, 128, 0);
+    I.persistent_blocks = (coop && e == cudaSuccess) ? per_sm * sms : 0;
+    cudaGetLastError();
+  }
   IMP_TRY(c, cudaMemset(I.res, 0, ns * sizeof(StepResult)));
   IMP_TRY(c, cudaMemset(c->prof.dev, 0, 3 * PROF_NCAT * sizeof(unsigned long long)));
   IMP_TRY(c, cudaMemcpy(I.m_own, M.f_m_own.data(), nf, cudaMemcpyHostToDevice));
@@ -894,6 +1101,12 @@ int bes_implicit_stats(const bes_ctx* ctx, int64_t* out) {
   out[1] = ctx->imp.host_syncs;
   out[2] = (int64_t)ctx->imp.counters_host[0];
   out[3] = (int64_t)ctx->imp.counters_host[1];
+  return BES_OK;
+}
+
+int bes_tuning(const bes_ctx* ctx, char* buf, size_t cap) {
+  if (!ctx || !buf || cap == 0) return BES_ERR_INVALID;
+  std::snprintf(buf, cap, "%s", ctx->imp.tuning.c_str());
   return BES_OK;
 }
 

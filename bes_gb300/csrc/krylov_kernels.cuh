@@ -26,6 +26,7 @@ struct SlotPtr {
   T* p;
   int64_t stride;
   __device__ __forceinline__ T* at() const { return p + (int64_t)blockIdx.y * stride; }
+  __device__ __forceinline__ T* of(int k) const { return p + (int64_t)k * stride; }
 };
 template <class T>
 inline SlotPtr<T> slots(T* p, int64_t stride) { return SlotPtr<T>{p, stride}; }
@@ -38,6 +39,14 @@ __device__ __forceinline__ bool slot_idle(const int32_t* run) {
 
 // ---- preconditioners ------------------------------------------------------------------------
 
+// Load of a Krylov vector entry; COH: through L2 only (ld.global.cg), for values that other
+// blocks of the same launch wrote (a persistent sweep: L1 is not coherent across SMs).
+template <bool COH, class T>
+__device__ __forceinline__ T vld(const T* p) {
+  if constexpr (COH) return __ldcg(p);
+  else return *p;
+}
+
 // Colour-ordered block-ILU(0) sweep when the colours are contiguous cell ranges in increasing
 // order (the colour-major numbering): the rows of one colour are [r0, r1), lower neighbours
 // are j < r0 and upper neighbours k >= r1, so no row list or position lookup is needed.  The
@@ -47,7 +56,7 @@ __device__ __forceinline__ bool slot_idle(const int32_t* run) {
 //   LOWER and UPPER   the last colour: both solves at once (it has no upper neighbours)
 //   UPPER only        colours C-2..0 of the backward sweep: out_i = inv(U_ii)(y_i - sum U_ik z_k)
 // `in` and `out` must not alias.
-template <class T, bool LOWER, bool UPPER>
+template <class T, bool LOWER, bool UPPER, bool COH = false>
 __device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, int r1, int s1,
                                                const T* __restrict__ A,
                                                const T* __restrict__ Dinv,
@@ -56,7 +65,7 @@ __device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, 
   const T* own = (LOWER || r0 == 0) ? in : out;
   T acc[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
+  for (int v = 0; v < 5; ++v) acc[v] = vld<COH>(own + (int64_t)i * 5 + v);
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const int j = m.adj[s * nc + i];
@@ -66,7 +75,7 @@ __device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, 
     const T* src = (lower && j < s1) ? in : out;
     T y[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) y[v] = src[(int64_t)j * 5 + v];
+    for (int v = 0; v < 5; ++v) y[v] = vld<COH>(src + (int64_t)j * 5 + v);
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -96,7 +105,7 @@ __global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int 
   ilu_colour_row<T, LOWER, UPPER>(m, i, r0, r1, s1, Ap.at(), Dp.at(), inp.at(), outp.at());
 }
 
-template <bool LOWER, bool UPPER>
+template <bool LOWER, bool UPPER, bool COH = false>
 __device__ __forceinline__ void ilu_colour_packed_row(
     const DevMesh& m, int i, int r0, int r1, int s1, const __half2* __restrict__ H,
     const float* __restrict__ HS, const __half2* __restrict__ D, const float* __restrict__ DS,
@@ -105,7 +114,7 @@ __device__ __forceinline__ void ilu_colour_packed_row(
   const float* own = (LOWER || r0 == 0) ? in : out;
   float acc[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
+  for (int v = 0; v < 5; ++v) acc[v] = vld<COH>(own + (int64_t)i * 5 + v);
   // the four neighbour ids first (one round trip), then the qualifying slots
   int jn[4];
 #pragma unroll
@@ -120,7 +129,7 @@ __device__ __forceinline__ void ilu_colour_packed_row(
     const float sc = HS[(int64_t)s * nc + i];
     float y[5], a[26];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) y[v] = sc * src[(int64_t)j * 5 + v];
+    for (int v = 0; v < 5; ++v) y[v] = sc * vld<COH>(src + (int64_t)j * 5 + v);
     load_packed(H, s, nc, i, a);
 #pragma unroll
     for (int r = 0; r < 5; ++r)
@@ -155,6 +164,128 @@ __global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
   if (i >= r1 || slot_idle(run)) return;
   ilu_colour_packed_row<LOWER, UPPER>(m, i, r0, r1, s1, Hp.at(), HSp.at(), Dp.at(), DSp.at(),
                                       inp.at(), outp.at());
+}
+
+// ---- persistent colour sweep ----------------------------------------------------------------
+// One launch per preconditioner application: a grid of resident blocks (cooperative launch,
+// sized by occupancy) walks the 2C-1 colour stages of the sweep in order, the rows of every
+// slot of a stage spread over all its threads, with a grid barrier between stages.  Each row
+// computes exactly what the per-colour kernels compute.  Vector values written in one stage
+// are read in later stages by other blocks, so those loads go through L2 (vld<true>).
+constexpr int kMaxStages = 16;
+struct SweepPlan {
+  int n;                     // stages
+  int s1;                    // end of colour 0
+  int r0[kMaxStages], r1[kMaxStages];
+  int kind[kMaxStages];      // 0 lower solve, 1 both solves (last colour), 2 upper solve
+};
+
+// Grid barrier state (device memory, zero at start): arrivals, generation, error flag.  A
+// wait gives up after one second (BES_ERR_TIMEOUT for the host), and once the error flag is
+// set every later wait of every launch returns at once, so no launch can hang.
+struct GridSync {
+  unsigned int* count;
+  unsigned int* gen;
+  int* error;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// All blocks of the grid arrive before any leaves; false if the wait gave up.
+__device__ __forceinline__ bool grid_sync(const GridSync& g) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int good = *(volatile int*)g.error == 0;
+    if (good) {
+      const unsigned g0 = ld_acquire(g.gen);
+      __threadfence();
+      const unsigned t = atomicAdd(g.count, 1u);
+      if (t == gridDim.x - 1) {
+        atomicExch(g.count, 0u);
+        __threadfence();
+        atomicAdd(g.gen, 1u);
+      } else {
+        const unsigned long long t0 = global_ns();
+        while (ld_acquire(g.gen) == g0) {
+          if (*(volatile int*)g.error) {
+            good = 0;
+            break;
+          }
+          if (global_ns() - t0 > 1000000000ull) {
+            atomicExch(g.error, 1);
+            good = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Operands of a sweep: the factors (packed 16-bit with scales, or T) and the vectors.
+template <class T>
+struct SweepOps {
+  SlotPtr<const __half2> H, D;   // packed: off-diagonal factor blocks, inverse diagonal
+  SlotPtr<const float> HS, DS;   // packed: their scales
+  SlotPtr<const T> L, Dinv;      // unpacked factors
+  SlotPtr<const T> in;
+  SlotPtr<T> out;
+};
+
+template <class T, bool PACKED>
+__global__ void __launch_bounds__(128) ilu_sweep_persistent_kernel(DevMesh m, SweepPlan P,
+                                                                   SweepOps<T> O, int nslot,
+                                                                   const int32_t* run,
+                                                                   GridSync gs) {
+  if (*(volatile int*)gs.error) return;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int st = 0; st < P.n; ++st) {
+    const int r0 = P.r0[st], r1 = P.r1[st], kind = P.kind[st];
+    const int nrows = r1 - r0;
+    const int64_t items = (int64_t)nslot * nrows;
+    for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items; it += nthreads) {
+      const int k = (int)(it / nrows);
+      const int i = r0 + (int)(it - (int64_t)k * nrows);
+      if (run != nullptr && run[k] == 0) continue;
+      if constexpr (PACKED) {
+        if (kind == 0)
+          ilu_colour_packed_row<true, false, true>(m, i, r0, r1, P.s1, O.H.of(k), O.HS.of(k),
+                                                   O.D.of(k), O.DS.of(k), O.in.of(k), O.out.of(k));
+        else if (kind == 1)
+          ilu_colour_packed_row<true, true, true>(m, i, r0, r1, P.s1, O.H.of(k), O.HS.of(k),
+                                                  O.D.of(k), O.DS.of(k), O.in.of(k), O.out.of(k));
+        else
+          ilu_colour_packed_row<false, true, true>(m, i, r0, r1, P.s1, O.H.of(k), O.HS.of(k),
+                                                   O.D.of(k), O.DS.of(k), O.in.of(k), O.out.of(k));
+      } else {
+        if (kind == 0)
+          ilu_colour_row<T, true, false, true>(m, i, r0, r1, P.s1, O.L.of(k), O.Dinv.of(k),
+                                               O.in.of(k), O.out.of(k));
+        else if (kind == 1)
+          ilu_colour_row<T, true, true, true>(m, i, r0, r1, P.s1, O.L.of(k), O.Dinv.of(k),
+                                              O.in.of(k), O.out.of(k));
+        else
+          ilu_colour_row<T, false, true, true>(m, i, r0, r1, P.s1, O.L.of(k), O.Dinv.of(k),
+                                               O.in.of(k), O.out.of(k));
+      }
+    }
+    if (st + 1 < P.n && !grid_sync(gs)) return;
+  }
 }
 
 // Level-scheduled block ILU(0) in reverse Cuthill-McKee order: forward solve of one stage,

@@ -30,6 +30,7 @@ EXPORTED = [
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
     "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
     "bes_implicit_stats", "bes_set_linear_guard", "bes_set_condition", "bes_implicit_sweep",
+    "bes_tuning",
     "bes_mlp_create", "bes_mlp_destroy", "bes_mlp_last_error", "bes_mlp_train", "bes_mlp_infer",
     "bes_mlp_init_state", "bes_mlp_params", "bes_mlp_features", "bes_mlp_loss_grad",
     "bes_mlp_apply_grad", "bes_mlp_normalisation",
@@ -73,7 +74,8 @@ class Options(ctypes.Structure):
         ("jacobian_repeat", ctypes.c_int32), ("precision", ctypes.c_int32),
         ("cfl_ramp_steps", ctypes.c_int32), ("freestream_ramp", ctypes.c_int32),
         ("cfl_ramp_start", ctypes.c_double), ("cfl_ramp_end", ctypes.c_double),
-        ("freestream_ramp_start_frac", ctypes.c_double), ("reserved", ctypes.c_double * 3),
+        ("freestream_ramp_start_frac", ctypes.c_double), ("sweep_kernel", ctypes.c_int32),
+        ("reserved_i", ctypes.c_int32), ("reserved", ctypes.c_double * 2),
     ]
 
 
@@ -140,6 +142,7 @@ def load(path: str = LIB_PATH):
                                 ctypes.POINTER(ctypes.c_int64), D]
     L.bes_implicit_stats.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_set_linear_guard.argtypes = [P, ctypes.c_int32]
+    L.bes_tuning.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
     L.bes_set_condition.argtypes = [P, ctypes.c_int32, D, D]
     L.bes_implicit_sweep.argtypes = [P, ctypes.c_int32, D, D, D, ctypes.c_double, ctypes.c_int64,
                                      ctypes.POINTER(ctypes.c_int64), D, D, D, D]
@@ -470,6 +473,12 @@ class Context:
         self._check(load().bes_implicit_stats(self.h, _i(out)))
         return dict(steps=int(out[0]), host_syncs=int(out[1]), arnoldi_steps=int(out[2]),
                     restart_cycles=int(out[3]))
+
+    def tuning(self) -> str:
+        """bes_tuning: the autotuner's candidates, their device times and its choices."""
+        buf = ctypes.create_string_buffer(4096)
+        self._check(load().bes_tuning(self.h, buf, len(buf)))
+        return buf.value.decode()
 
     def set_linear_guard(self, max_cycles: int):
         """bes_set_linear_guard: restart-cycle limit of one linear solve (0: default)."""

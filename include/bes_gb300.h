@@ -87,7 +87,12 @@ typedef struct {
                                      ramps up (src/Config.cpp:688-706), 0 off */
   double cfl_ramp_start, cfl_ramp_end;
   double freestream_ramp_start_frac;  /* FREESTREAM_RAMP_START_FRAC (default 0.5) */
-  double reserved[3];
+  int32_t sweep_kernel;           /* SWEEP_KERNEL (additive): block-ILU(0) colour sweeps as
+                                     0 the autotuner's choice (timed on the first step's
+                                     system, see bes_tuning), 1 one launch per colour, 2 one
+                                     persistent launch per sweep */
+  int32_t reserved_i;
+  double reserved[2];
 } bes_options;
 
 typedef struct bes_ctx bes_ctx;
@@ -160,6 +165,10 @@ int bes_implicit_steps(bes_ctx* ctx, int64_t n, double* history);
  * bes_implicit_steps (one per step), out[2] Arnoldi steps and out[3] restart cycles the device
  * ran (each counted once per batched launch, whatever the number of conditions).  out [4]. */
 int bes_implicit_stats(const bes_ctx* ctx, int64_t* out);
+
+/* The implicit path's tuning report: for each tuned choice, the candidates with their measured
+ * device times and the one taken (one line each).  Empty until the first implicit step. */
+int bes_tuning(const bes_ctx* ctx, char* buf, size_t cap);
 
 /* Limit of restart cycles per linear solve (0: linear_solver_max_iter + 1, more than a solve
  * can take).  A solve that reaches the limit stops with its current iterate and the step
