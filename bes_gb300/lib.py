@@ -30,7 +30,7 @@ EXPORTED = [
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
     "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
     "bes_implicit_stats", "bes_set_linear_guard", "bes_set_condition", "bes_implicit_sweep",
-    "bes_tuning",
+    "bes_tuning", "bes_fp64_fma_rate",
     "bes_mlp_create", "bes_mlp_destroy", "bes_mlp_last_error", "bes_mlp_train", "bes_mlp_infer",
     "bes_mlp_init_state", "bes_mlp_params", "bes_mlp_features", "bes_mlp_loss_grad",
     "bes_mlp_apply_grad", "bes_mlp_normalisation",
@@ -143,6 +143,7 @@ def load(path: str = LIB_PATH):
     L.bes_implicit_stats.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.bes_set_linear_guard.argtypes = [P, ctypes.c_int32]
     L.bes_tuning.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+    L.bes_fp64_fma_rate.argtypes = [D]
     L.bes_set_condition.argtypes = [P, ctypes.c_int32, D, D]
     L.bes_implicit_sweep.argtypes = [P, ctypes.c_int32, D, D, D, ctypes.c_double, ctypes.c_int64,
                                      ctypes.POINTER(ctypes.c_int64), D, D, D, D]
@@ -262,6 +263,15 @@ class _MeshKeep:
                             self.tets.shape[0],
                             self.tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                             2 if self.tets.shape[1] == 3 else 3)
+
+
+def fp64_fma_rate() -> float:
+    """bes_fp64_fma_rate: FP64 FMA per second of the current device."""
+    r = ctypes.c_double()
+    rc = load().bes_fp64_fma_rate(ctypes.byref(r))
+    if rc:
+        raise BesError(rc, "bes_fp64_fma_rate failed")
+    return r.value
 
 
 def _i(a):

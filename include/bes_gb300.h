@@ -339,6 +339,10 @@ int bes_mlp_normalisation(const bes_mlp* mlp, double* out);
  * out[4] linear iterations whose Gram-Schmidt step needed the second pass.  out [5]. */
 int bes_counters(const bes_ctx* ctx, int64_t* out);
 
+/* FP64 fused multiply-add rate of the current device (FMA per second), measured with
+ * independent FMA chains on every SM: the denominator of the explicit kernels' roofline. */
+int bes_fp64_fma_rate(double* fma_per_s);
+
 /* Library build identification (e.g. "sm_103a"). */
 const char* bes_build_info(void);
 

@@ -13,7 +13,7 @@ KEYS = {"impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_
         "e2e"}
 
 
-@pytest.mark.parametrize("workload", ["explicit_bump_72k", "implicit_bump_2m"])
+@pytest.mark.parametrize("workload", ["explicit_bump_72k", "implicit_bump_72k"])
 def test_reference_arm_prints_the_contract_line(workload):
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
                           "--workload", workload, "--steps", "1", "--warmup", "1"],
@@ -24,6 +24,7 @@ def test_reference_arm_prints_the_contract_line(workload):
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["config"]["cells"] == 72000  # the workload's own mesh
 
 
 def _max_rank(rank, world, port, q):
