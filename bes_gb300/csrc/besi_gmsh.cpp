@@ -461,3 +461,48 @@ extern "C" int bes_host_geometry(const bes_mesh_arrays* mesh, int32_t muscl_face
   }
   return BES_OK;
 }
+
+namespace {
+// FNV-1a over the bytes of an array
+template <class T>
+uint64_t digest_of(const std::vector<T>& v) {
+  uint64_t h = 1469598103934665603ull;
+  const unsigned char* p = reinterpret_cast<const unsigned char*>(v.data());
+  for (size_t i = 0; i < v.size() * sizeof(T); ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h ^ (uint64_t)v.size();
+}
+}  // namespace
+
+extern "C" int bes_host_layout_digest(const bes_mesh_arrays* mesh, int32_t muscl_face_vector,
+                                      int32_t rcm_ilu_order, uint64_t* digests, int32_t cap,
+                                      int32_t* n, char* err, size_t err_cap) {
+  if (!mesh || !n) return BES_ERR_INVALID;
+  bes::RefMesh M;
+  std::string e;
+  if (!bes::build_ref_mesh(mesh->nodes, mesh->n_nodes, mesh->btris, mesh->btags, mesh->n_btris,
+                           mesh->tets, mesh->n_tets, bes_mesh_dim(mesh), muscl_face_vector != 0,
+                           M, e)) {
+    set_err(err, err_cap, e);
+    return BES_ERR_MESH;
+  }
+  bes::SoaMesh S;
+  bes::build_soa(M, 5.0, muscl_face_vector != 0, true, S);
+  if (rcm_ilu_order) bes::build_ilu_schedule(S, true);
+  const uint64_t d[] = {
+      digest_of(S.cell_new2ref), digest_of(S.cell_ref2new), digest_of(S.face_new2ref),
+      digest_of(S.face_ref2new), digest_of(S.vol), digest_of(S.inv_vol), digest_of(S.eps2),
+      digest_of(S.plen), digest_of(S.adj), digest_of(S.cface), digest_of(S.gface),
+      digest_of(S.Sc), digest_of(S.w), digest_of(S.r), digest_of(S.cflags),
+      digest_of(S.extra_cell), digest_of(S.extra_m), digest_of(S.fown), digest_of(S.fnb),
+      digest_of(S.fsrc_own), digest_of(S.fsrc_nb), digest_of(S.fn), digest_of(S.farea),
+      digest_of(S.f_m_own), digest_of(S.f_m_nb), digest_of(S.cell_color), digest_of(S.ilu_pos),
+      digest_of(S.stage_rows), digest_of(S.stage_off), digest_of(S.rcm_rank)};
+  const int32_t k = (int32_t)(sizeof(d) / sizeof(d[0]));
+  *n = k;
+  if (digests)
+    for (int32_t i = 0; i < k && i < cap; ++i) digests[i] = d[i];
+  return BES_OK;
+}

@@ -30,7 +30,7 @@ EXPORTED = [
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
     "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
     "bes_implicit_stats", "bes_set_linear_guard", "bes_set_condition", "bes_implicit_sweep",
-    "bes_tuning", "bes_fp64_fma_rate",
+    "bes_tuning", "bes_fp64_fma_rate", "bes_host_layout_digest",
     "bes_mlp_create", "bes_mlp_destroy", "bes_mlp_last_error", "bes_mlp_train", "bes_mlp_infer",
     "bes_mlp_init_state", "bes_mlp_params", "bes_mlp_features", "bes_mlp_loss_grad",
     "bes_mlp_apply_grad", "bes_mlp_normalisation",
@@ -144,6 +144,10 @@ def load(path: str = LIB_PATH):
     L.bes_set_linear_guard.argtypes = [P, ctypes.c_int32]
     L.bes_tuning.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
     L.bes_fp64_fma_rate.argtypes = [D]
+    L.bes_host_layout_digest.argtypes = [ctypes.POINTER(MeshArrays), ctypes.c_int32,
+                                         ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
+                                         ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.c_char_p, ctypes.c_size_t]
     L.bes_set_condition.argtypes = [P, ctypes.c_int32, D, D]
     L.bes_implicit_sweep.argtypes = [P, ctypes.c_int32, D, D, D, ctypes.c_double, ctypes.c_int64,
                                      ctypes.POINTER(ctypes.c_int64), D, D, D, D]
@@ -276,6 +280,20 @@ def fp64_fma_rate() -> float:
 
 def _i(a):
     return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def host_layout_digest(mesh, muscl_exact: bool = False, rcm_ilu_order: bool = False) -> list:
+    """bes_host_layout_digest: 64-bit digests of every device-layout array of the mesh build."""
+    L = load()
+    keep = _MeshKeep(mesh)
+    n = ctypes.c_int32()
+    err = ctypes.create_string_buffer(512)
+    out = (ctypes.c_uint64 * 64)()
+    rc = L.bes_host_layout_digest(ctypes.byref(keep.c), int(muscl_exact), int(rcm_ilu_order),
+                                  out, 64, ctypes.byref(n), err, 512)
+    if rc != BES_OK:
+        raise BesError(rc, err.value.decode())
+    return [int(out[i]) for i in range(n.value)]
 
 
 def host_geometry(mesh, muscl_exact: bool = False) -> dict:

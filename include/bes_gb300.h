@@ -412,6 +412,15 @@ int bes_host_geometry(const bes_mesh_arrays* mesh, int32_t muscl_face_vector, in
                       int64_t* face_kind, int64_t* muscl_slot, int64_t* cell_new2ref,
                       int64_t* face_new2ref, char* err, size_t err_cap);
 
+/* Host-only (no GPU): 64-bit digests (FNV-1a) of every device-layout array the mesh build
+ * produces (numbering, cell and face arrays, ELL slots, colouring and the block-ILU(0)
+ * schedule; rcm_ilu_order 1: the level-scheduled RCM order), so that builds on different
+ * thread counts or hosts can be compared array for array.  *n receives the count (30);
+ * digests [cap] may be NULL. */
+int bes_host_layout_digest(const bes_mesh_arrays* mesh, int32_t muscl_face_vector,
+                           int32_t rcm_ilu_order, uint64_t* digests, int32_t cap, int32_t* n,
+                           char* err, size_t err_cap);
+
 #ifdef __cplusplus
 }
 #endif

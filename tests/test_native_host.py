@@ -238,14 +238,19 @@ def test_besi_parser_is_strict(line):
 
 def test_host_build_is_independent_of_the_thread_count():
     """The host mesh build runs its independent per-cell and per-face loops on several threads;
-    one thread gives the same geometry and numbering (BES_HOST_THREADS is read once per
-    process, so each count runs in a process of its own)."""
+    one thread gives the same geometry and numbering, and every device-layout array (weights,
+    face lists, ELL slots, colouring, both block-ILU(0) schedules) byte for byte
+    (BES_HOST_THREADS is read once per process, so each count runs in a process of its own)."""
     import json
     import subprocess
     import sys
-    code = ("import json, sys; sys.path.insert(0, %r); from bes_gb300 import lib, meshgen; "
-            "g = lib.host_geometry(meshgen.gaussian_box(40, 20, 40, 1.05)); "
-            "print(json.dumps({k: v.ravel().tolist()[::97] for k, v in g.items()}))"
+    code = ("import json, sys, hashlib; sys.path.insert(0, %r); from bes_gb300 import lib, meshgen; "
+            "m = meshgen.gaussian_box(40, 20, 40, 1.05); g = lib.host_geometry(m); "
+            "d = {k: hashlib.sha256(v.tobytes()).hexdigest() for k, v in g.items()}; "
+            "d['layout'] = lib.host_layout_digest(m); "
+            "d['layout_rcm'] = lib.host_layout_digest(m, rcm_ilu_order=True); "
+            "d['layout_exact'] = lib.host_layout_digest(m, muscl_exact=True); "
+            "print(json.dumps(d))"
             % os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     outs = []
     for n in ("1", "8"):
@@ -253,4 +258,5 @@ def test_host_build_is_independent_of_the_thread_count():
                            env=dict(os.environ, BES_HOST_THREADS=n), timeout=300)
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append(json.loads(r.stdout.strip().splitlines()[-1]))
+    assert len(outs[0]["layout"]) == 30
     assert outs[0] == outs[1]
