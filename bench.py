@@ -554,6 +554,7 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
                     "h2d_bytes_per_step": 40 * nc, "d2h_bytes_per_step": 40 * nc},
             "gpu_launches": mixed["launches"],
             "host_syncs_per_step": mixed["host_syncs_per_step"],
+            "tuning": ctx.tuning().strip(),
             "restart_cycles_per_step": mixed["restart_cycles_per_step"],
             "roofline": {"kernel": KERNEL_NAMES[dom][prec],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -813,6 +814,7 @@ def run_isweep(args, wl, torch, mesh, clocks):
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     s1 = cb.implicit_stats()
+    tuning = cb.tuning().strip()
     cb.close()
     clk = clocks.stop()
     conv_p = p["final_res"] <= 1e-8
@@ -847,6 +849,7 @@ def run_isweep(args, wl, torch, mesh, clocks):
                 "seconds": {"batched_fp32_system": t_batch, "plain_fp64": t_plain},
                 "batched_steps_per_condition": [int(x) for x in b["steps"]],
                 "host_syncs": s1["host_syncs"] - s0["host_syncs"],
+                "tuning": tuning,
                 "max_force_coefficient_abs_diff": (max(r["force_coefficient_abs_diff"] for r in both)
                                                    if both else None),
                 "target": "1e-8 x each condition's first residual L2 (both start from the "

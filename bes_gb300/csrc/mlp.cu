@@ -13,8 +13,9 @@
 //   4 hidden layers of width 256: z = h W^T + b; [gamma, beta] = c F^T + g;
 //             y = z (1 + gamma) + beta; h = silu(y);
 //   output    o = h W4^T + b4 (5 values) = (U - U_inf(c)) / scale.
-// GEMMs run on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation) with
-// BF16 copies of the weights and of the activations that feed them; everything else is FP32;
+// GEMMs run on the fifth-generation tensor cores (tcgen05.mma, BF16 operands, FP32
+// accumulation in tensor memory) with BF16 copies of the weights and of the activations that
+// feed them; everything else is FP32;
 // AdamW keeps FP32 master weights.  All reductions are in a fixed order (no atomics), so a
 // run is reproducible bit for bit.
 #include <cuda_bf16.h>
@@ -73,110 +74,178 @@ __device__ __forceinline__ float dsilu(float y) {
   return s * (1.0f + y * (1.0f - s));
 }
 
-// ---- tensor-core GEMM ------------------------------------------------------------------------
+// ---- tensor-core GEMM (tcgen05, accumulator in tensor memory) ----------------------------------
 // C[z][m][n] = sum over k in split z of A(m,k) B(k,n), FP32 out, with
 //   A(m,k) = A_T ? A[k*lda + m] : A[m*lda + k]
 //   B(k,n) = B_T ? B[k*ldb + n] : B[n*ldb + k]
-// M % 128 == 0, N % 64 == 0, k_split % 32 == 0 (checked by the caller).  Tiles 128 x 64 x 32,
-// eight warps of 32 x 32; shared tiles are stored m-major / n-major with k contiguous so that
-// ldmatrix yields the mma.sync fragments directly.
-constexpr int GBM = 128, GBN = 64, GBK = 32, GPAD = 8;
+// M % 128 == 0, N % 64 == 0, k_split % 64 == 0 (checked by the caller).  One CTA of 128
+// threads computes a 128 x 64 tile of C: per 64-wide slice of k, all threads stage the A and B
+// slices in shared memory as K-major 8x8 core matrices (no swizzle; an MN-major operand is
+// transposed while it is staged), one thread issues four tcgen05.mma (M 128, N 64, K 16, BF16
+// operands, FP32 accumulation in 64 columns of tensor memory) and commits them to an
+// mbarrier; after the last slice each warp reads its 32 accumulator rows back with
+// tcgen05.ld.  Every wait on the mbarrier gives up after two seconds and sets *err.
+constexpr int GBM = 128, GBN = 64, GBK = 64;
+constexpr int kCoreBytes = 128;                  // an 8 x 8 core matrix of 16-bit values
+constexpr int kSbo = (GBK / 8) * kCoreBytes;     // next 8-row group: one k-slice of cores
+constexpr int kLbo = kCoreBytes;                 // next 8 values of k
 
-__device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* p) {
-  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(a));
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
-                                         uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+// shared-memory matrix descriptor: K-major, no swizzle, start address and the two strides
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((kLbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((kSbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of this architecture
+  return d;                // base offset 0, layout type 0 (no swizzle)
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ unsigned long long ns_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// wait for phase `parity` of the mbarrier; false after two seconds
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  const unsigned long long t0 = ns_now();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (ns_now() - t0 > 2000000000ull) return false;
+  }
+}
+
+// stage a ROWS x 64 (k) slice, rows r0.., k0.., into K-major core matrices: value (r, k) at
+// byte (r/8)*kSbo + (k/8)*kLbo + (r%8)*16 + (k%8)*2.  The source is k-contiguous by rows
+// (src[r*ld + k]) when !TR, or row-contiguous by k (src[k*ld + r]) when TR.
+template <bool TR, int ROWS>
+__device__ __forceinline__ void stage_slice(uint8_t* sm, const bf16* __restrict__ src, int ld,
+                                            int r0, int k0) {
+  if (!TR) {
+    // 16-byte pieces: row r, values k..k+7 (one core-matrix row)
+    for (int v = threadIdx.x; v < ROWS * (GBK / 8); v += blockDim.x) {
+      const int r = v / (GBK / 8), seg = v % (GBK / 8);
+      const uint4 x = *reinterpret_cast<const uint4*>(src + (size_t)(r0 + r) * ld + k0 + seg * 8);
+      *reinterpret_cast<uint4*>(sm + (r / 8) * kSbo + seg * kLbo + (r % 8) * 16) = x;
+    }
+  } else {
+    // 16-byte pieces along the rows (k fixed, rows r..r+7), scattered to eight core rows
+    for (int v = threadIdx.x; v < GBK * (ROWS / 8); v += blockDim.x) {
+      const int k = v / (ROWS / 8), rs = v % (ROWS / 8);
+      const uint4 x = *reinterpret_cast<const uint4*>(src + (size_t)(k0 + k) * ld + r0 + rs * 8);
+      const uint16_t* e = reinterpret_cast<const uint16_t*>(&x);
+      uint8_t* base = sm + rs * kSbo + (k / 8) * kLbo + (k % 8) * 2;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) *reinterpret_cast<uint16_t*>(base + q * 16) = e[q];
+    }
+  }
 }
 
 template <bool A_T, bool B_T>
-__global__ void __launch_bounds__(256) gemm_bf16_kernel(int M, int N, const bf16* __restrict__ A,
-                                                        int lda, const bf16* __restrict__ B,
-                                                        int ldb, float* __restrict__ C, int ldc,
-                                                        int k_split) {
-  __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];
-  __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp & 3, wn = warp >> 2;
+__global__ void __launch_bounds__(128) gemm_tc_kernel(int M, int N, const bf16* __restrict__ A,
+                                                      int lda, const bf16* __restrict__ B,
+                                                      int ldb, float* __restrict__ C, int ldc,
+                                                      int k_split, int* __restrict__ err) {
+  __shared__ __align__(128) uint8_t As[GBM * GBK * 2];
+  __shared__ __align__(128) uint8_t Bs[GBN * GBK * 2];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
   const int k_begin = blockIdx.z * k_split, k_end = k_begin + k_split;
   C += (size_t)blockIdx.z * M * ldc;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.0f;
-  for (int k0 = k_begin; k0 < k_end; k0 += GBK) {
-    // A tile: 128 x 32
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const int v = tid + i * 256;
-      if (!A_T) {
-        const int row = v >> 2, seg = v & 3;
-        *reinterpret_cast<uint4*>(&As[row][seg * 8]) =
-            *reinterpret_cast<const uint4*>(A + (size_t)(m0 + row) * lda + k0 + seg * 8);
-      } else {
-        const int kk = v >> 4, ms = v & 15;
-        const uint4 x = *reinterpret_cast<const uint4*>(A + (size_t)(k0 + kk) * lda + m0 + ms * 8);
-        const bf16* e = reinterpret_cast<const bf16*>(&x);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) As[ms * 8 + q][kk] = e[q];
-      }
-    }
-    // B tile: 64 (n) x 32 (k)
-    if (!B_T) {
-      const int row = tid >> 2, seg = tid & 3;
-      *reinterpret_cast<uint4*>(&Bs[row][seg * 8]) =
-          *reinterpret_cast<const uint4*>(B + (size_t)(n0 + row) * ldb + k0 + seg * 8);
-    } else {
-      const int kk = tid >> 3, ns = tid & 7;
-      const uint4 x = *reinterpret_cast<const uint4*>(B + (size_t)(k0 + kk) * ldb + n0 + ns * 8);
-      const bf16* e = reinterpret_cast<const bf16*>(&x);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) Bs[ns * 8 + q][kk] = e[q];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < GBK; ks += 16) {
-      uint32_t a[2][4], b[2][4];
-#pragma unroll
-      for (int mi = 0; mi < 2; ++mi)
-        ldmatrix_x4(a[mi], &As[wm * 32 + mi * 16 + (lane & 7) + ((lane >> 3) & 1) * 8]
-                               [ks + (lane >> 4) * 8]);
-#pragma unroll
-      for (int p = 0; p < 2; ++p)
-        ldmatrix_x4(b[p], &Bs[wn * 32 + p * 16 + (lane & 7) + (lane >> 4) * 8]
-                             [ks + ((lane >> 3) & 1) * 8]);
-#pragma unroll
-      for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-        for (int nj = 0; nj < 4; ++nj)
-          mma_bf16(acc[mi][nj], a[mi], b[nj >> 1][(nj & 1) * 2], b[nj >> 1][(nj & 1) * 2 + 1]);
-    }
-    __syncthreads();
+  const uint32_t mb = smem_u32(&mbar);
+  if (warp == 0) {
+    // 64 columns of tensor memory for the 128 x 64 FP32 accumulator
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n"
+                 :: "r"(smem_u32(&tmem_base)) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
-  const int g = lane >> 2, t = lane & 3;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t idesc = umma_idesc(GBM, GBN);
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int k0 = k_begin; k0 < k_end && ok; k0 += GBK) {
+    stage_slice<A_T, GBM>(As, A, lda, m0, k0);
+    stage_slice<B_T, GBN>(Bs, B, ldb, n0, k0);
+    // the staged values (generic proxy) become visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
-  for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-    for (int nj = 0; nj < 4; ++nj) {
-      const int r = m0 + wm * 32 + mi * 16 + g;
-      const int c = n0 + wn * 32 + nj * 8 + 2 * t;
-      *reinterpret_cast<float2*>(&C[(size_t)r * ldc + c]) = make_float2(acc[mi][nj][0], acc[mi][nj][1]);
-      *reinterpret_cast<float2*>(&C[(size_t)(r + 8) * ldc + c]) =
-          make_float2(acc[mi][nj][2], acc[mi][nj][3]);
+      for (int kk = 0; kk < GBK / 16; ++kk) {
+        // K = 16 per instruction: two core matrices along k
+        const uint64_t ad = umma_desc(smem_u32(As) + kk * 2 * kLbo);
+        const uint64_t bd = umma_desc(smem_u32(Bs) + kk * 2 * kLbo);
+        const uint32_t acc = (k0 > k_begin || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+            :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc) : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
+          :: "r"(mb) : "memory");
     }
+    // the slice's products are done before its shared memory is staged again; the verdict
+    // is the same for every thread (tcgen05.ld below is a warp-synchronous instruction)
+    const int waited = mbar_wait(mb, phase) ? 1 : 0;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    ok = __syncthreads_and(waited) != 0;
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    phase ^= 1;
+  }
+  if (ok) {
+    // each warp reads its 32 rows (tensor-memory lanes 32 w .. 32 w + 31), 16 columns a time
+#pragma unroll
+    for (int c0 = 0; c0 < GBN; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+          "%13,%14,%15}, [%16];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+            "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+            "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      float* dst = C + (size_t)(m0 + warp * 32 + lane) * ldc + n0 + c0;
+#pragma unroll
+      for (int q = 0; q < 16; q += 4)
+        *reinterpret_cast<float4*>(dst + q) =
+            make_float4(__uint_as_float(r[q]), __uint_as_float(r[q + 1]),
+                        __uint_as_float(r[q + 2]), __uint_as_float(r[q + 3]));
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" :: "r"(tmem) : "memory");
 }
 
 // ---- elementwise and reduction kernels -------------------------------------------------------
@@ -438,6 +507,7 @@ struct bes_mlp {
   bf16* dZ = nullptr;
   float *part = nullptr, *red = nullptr, *wpart = nullptr;
   double* loss_part = nullptr;
+  int* gemm_err = nullptr;   // set by a GEMM whose tensor-core wait gave up
   std::vector<bes_mlp*> dummy;
 };
 
@@ -451,6 +521,16 @@ namespace {
       return BES_ERR_CUDA;                                                       \
     }                                                                            \
   } while (0)
+
+// BES_ERR_TIMEOUT (and the flag cleared) if a GEMM's wait on the tensor core gave up
+int gemm_status(bes_mlp* h) {
+  int e = 0;
+  MLP_TRY(h, cudaMemcpy(&e, h->gemm_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!e) return BES_OK;
+  cudaMemset(h->gemm_err, 0, sizeof(int));
+  h->last_error = "a tensor-core GEMM stopped waiting for its products after two seconds";
+  return BES_ERR_TIMEOUT;
+}
 
 template <class X>
 int mlp_alloc(bes_mlp* h, X** ptr, size_t count) {
@@ -495,9 +575,9 @@ inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
 // C = A(m,k) B(k,n) with optional split over k (partials at C + z*M*ldc)
 template <bool A_T, bool B_T>
 void gemm(cudaStream_t s, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb,
-          float* C, int ldc, int splits) {
+          float* C, int ldc, int splits, int* err) {
   dim3 grid(N / GBN, M / GBM, splits);
-  gemm_bf16_kernel<A_T, B_T><<<grid, 256, 0, s>>>(M, N, A, lda, B, ldb, C, ldc, K / splits);
+  gemm_tc_kernel<A_T, B_T><<<grid, 128, 0, s>>>(M, N, A, lda, B, ldb, C, ldc, K / splits, err);
 }
 
 // forward of B rows whose features are in h->H[0] and conditions in h->C; outputs in h->O
@@ -506,7 +586,7 @@ void forward(bes_mlp* h, int B) {
   const int fb = std::min(B, 4096);
   for (int l = 0; l < kLayers; ++l) {
     const int k = l == 0 ? kK0 : kW;
-    gemm<false, false>(s, B, kW, k, h->H[l], k, h->Wb[l], k, h->Z[l], kW, 1);
+    gemm<false, false>(s, B, kW, k, h->H[l], k, h->Wb[l], k, h->Z[l], kW, 1, h->gemm_err);
     film_forward_kernel<<<fb, kW, 0, s>>>(B, h->Z[l], h->p + h->L.b[l], h->p + h->L.F[l],
                                           h->p + h->L.g[l], h->C, h->Y[l], h->H[l + 1]);
   }
@@ -533,13 +613,13 @@ void backward(bes_mlp* h, int B) {
                                               h->grad + L.g[l]);
     // dW_l = dZ^T H_l, split over the rows in chunks of 512 when they divide the batch
     const int splits = B % 512 == 0 ? B / 512 : 1;
-    gemm<true, true>(s, kW, k, B, h->dZ, kW, h->H[l], k, h->wpart, k, splits);
+    gemm<true, true>(s, kW, k, B, h->dZ, kW, h->H[l], k, h->wpart, k, splits, h->gemm_err);
     reduce_chunks_kernel<<<nblk((int64_t)kW * k, 256), 256, 0, s>>>(splits, kW * k, h->wpart,
                                                                     h->grad + L.W[l]);
     if (l > 0) {
       // dH_l = dZ W_l (W_l is [256][256], element (k, n) at k*256 + n)
       float* dHout = dHin == h->dH ? h->dHk : h->dH;
-      gemm<false, true>(s, B, kW, kW, h->dZ, kW, h->Wb[l], kW, dHout, kW, 1);
+      gemm<false, true>(s, B, kW, kW, h->dZ, kW, h->Wb[l], kW, dHout, kW, 1, h->gemm_err);
       dHin = dHout;
     }
   }
@@ -615,10 +695,12 @@ int bes_mlp_create(const bes_ctx* ctx, uint64_t seed, bes_mlp** out) {
   rc |= mlp_alloc(h, &h->v, L.n);
   rc |= mlp_alloc(h, &h->decay, L.n);
   for (int l = 0; l < kLayers; ++l) rc |= mlp_alloc(h, &h->Wb[l], (size_t)kW * (l == 0 ? kK0 : kW));
+  rc |= mlp_alloc(h, &h->gemm_err, 1);
   if (rc) {
     bes_mlp_destroy(h);
     return BES_ERR_CUDA;
   }
+  cudaMemset(h->gemm_err, 0, sizeof(int));
   // Glorot-uniform weights from the seed, zero biases, identity FiLM (F = 0, g = 0), a small
   // output layer
   std::vector<float> p(L.n, 0.0f);
@@ -724,7 +806,7 @@ int bes_mlp_loss_grad(bes_mlp* h, int32_t n_rows, const int64_t* cells, const do
   if (outputs)
     for (int r = 0; r < B; ++r)
       for (int v = 0; v < kOut; ++v) outputs[r * kOut + v] = o[r * 8 + v];
-  return BES_OK;
+  return gemm_status(h);
 }
 
 int bes_mlp_apply_grad(bes_mlp* h, const float* grad, double lr, double weight_decay) {
@@ -815,7 +897,7 @@ int bes_mlp_train(bes_mlp* h, int32_t n_samples, const double* mach, const doubl
     h->last_error = std::string("training: ") + cudaGetErrorString(e);
     return BES_ERR_CUDA;
   }
-  return BES_OK;
+  return gemm_status(h);
 }
 
 int bes_mlp_infer(bes_mlp* h, int32_t n, const double* mach, double* U) {
@@ -847,7 +929,7 @@ int bes_mlp_infer(bes_mlp* h, int32_t n, const double* mach, double* U) {
     }
   }
   MLP_TRY(h, cudaGetLastError());
-  return BES_OK;
+  return gemm_status(h);
 }
 
 int bes_mlp_init_state(bes_mlp* h, bes_ctx* ctx, int32_t* used) {
