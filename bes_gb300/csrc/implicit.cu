@@ -275,23 +275,35 @@ void enqueue_precond(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> in, co
           auto HS = cslots((const float*)S.LUs, 4LL * S.nc);
           auto D = cslots((const __half2*)S.D16, 13LL * S.nc);
           auto DS = cslots((const float*)S.Ds, (int64_t)S.nc);
-          if (lower && !upper)
-            ilu_colour_packed_kernel<true, false><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run);
-          else if (lower)
-            ilu_colour_packed_kernel<true, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run);
-          else
-            ilu_colour_packed_kernel<false, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run);
+#define BES_PACKED_SWEEP(LO, UP, BA) \
+  ilu_colour_packed_kernel<LO, UP, BA><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run)
+          if (S.nslot > 1) {
+            if (lower && !upper) BES_PACKED_SWEEP(true, false, true);
+            else if (lower) BES_PACKED_SWEEP(true, true, true);
+            else BES_PACKED_SWEEP(false, true, true);
+          } else {
+            if (lower && !upper) BES_PACKED_SWEEP(true, false, false);
+            else if (lower) BES_PACKED_SWEEP(true, true, false);
+            else BES_PACKED_SWEEP(false, true, false);
+          }
+#undef BES_PACKED_SWEEP
           return;
         }
       }
       auto L = cslots((const T*)S.LU, S.sA);
       auto D = cslots((const T*)S.Dinv, S.sDinv);
-      if (lower && !upper)
-        ilu_colour_kernel<T, true, false><<<grid, 128, 0, s>>>(m, r0, r1, s1, L, D, in, Z, run);
-      else if (lower)
-        ilu_colour_kernel<T, true, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, L, D, in, Z, run);
-      else
-        ilu_colour_kernel<T, false, true><<<grid, 128, 0, s>>>(m, r0, r1, s1, L, D, in, Z, run);
+#define BES_SWEEP(LO, UP, BA) \
+  ilu_colour_kernel<T, LO, UP, BA><<<grid, 128, 0, s>>>(m, r0, r1, s1, L, D, in, Z, run)
+      if (S.nslot > 1) {
+        if (lower && !upper) BES_SWEEP(true, false, true);
+        else if (lower) BES_SWEEP(true, true, true);
+        else BES_SWEEP(false, true, true);
+      } else {
+        if (lower && !upper) BES_SWEEP(true, false, false);
+        else if (lower) BES_SWEEP(true, true, false);
+        else BES_SWEEP(false, true, false);
+      }
+#undef BES_SWEEP
     };
     for (int k = 1; k < C - 1; ++k) launch(k, true, false);
     launch(C - 1, true, true);
@@ -321,12 +333,19 @@ void enqueue_spmv(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> x, SlotPt
   const dim3 grid(nblk(S.nc, 256), S.nslot);
   if constexpr (std::is_same<T, float>::value) {
     if (S.packed) {
-      spmv_packed_kernel<<<grid, 256, 0, s>>>(S.c->dm, cslots((const __half2*)S.A16, 65LL * S.nc),
-                                              cslots((const float*)S.As, 5LL * S.nc), x, b, y, run);
+      auto H = cslots((const __half2*)S.A16, 65LL * S.nc);
+      auto Sc = cslots((const float*)S.As, 5LL * S.nc);
+      if (S.nslot > 1)
+        spmv_packed_kernel<true><<<grid, 256, 0, s>>>(S.c->dm, H, Sc, x, b, y, run);
+      else
+        spmv_packed_kernel<false><<<grid, 256, 0, s>>>(S.c->dm, H, Sc, x, b, y, run);
       return;
     }
   }
-  spmv_kernel<T><<<grid, 256, 0, s>>>(S.c->dm, cslots((const T*)S.A, S.sA), x, b, y, run);
+  if (S.nslot > 1)
+    spmv_kernel<T, true><<<grid, 256, 0, s>>>(S.c->dm, cslots((const T*)S.A, S.sA), x, b, y, run);
+  else
+    spmv_kernel<T, false><<<grid, 256, 0, s>>>(S.c->dm, cslots((const T*)S.A, S.sA), x, b, y, run);
 }
 
 // Body of the IF node of Arnoldi step j (slots with a running cycle): w = A M^{-1} v_j,

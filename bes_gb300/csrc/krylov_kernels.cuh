@@ -33,6 +33,15 @@ inline SlotPtr<T> slots(T* p, int64_t stride) { return SlotPtr<T>{p, stride}; }
 template <class T>
 inline SlotPtr<const T> cslots(const T* p, int64_t stride) { return SlotPtr<const T>{p, stride}; }
 
+// The slot's array: with BATCH false (a single-condition context) the first slot's pointer
+// itself, so that the hot gather kernels keep their pointers in the parameter bank instead of
+// computing per-slot addresses into registers.
+template <bool BATCH, class T>
+__device__ __forceinline__ T* sat(const SlotPtr<T>& s) {
+  if constexpr (BATCH) return s.at();
+  else return s.p;
+}
+
 __device__ __forceinline__ bool slot_idle(const int32_t* run) {
   return run != nullptr && run[blockIdx.y] == 0;
 }
@@ -95,14 +104,15 @@ __device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, 
   }
 }
 
-template <class T, bool LOWER, bool UPPER>
+template <class T, bool LOWER, bool UPPER, bool BATCH>
 __global__ void __launch_bounds__(128) ilu_colour_kernel(DevMesh m, int r0, int r1, int s1,
                                                          SlotPtr<const T> Ap, SlotPtr<const T> Dp,
                                                          SlotPtr<const T> inp, SlotPtr<T> outp,
                                                          const int32_t* run) {
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1 || slot_idle(run)) return;
-  ilu_colour_row<T, LOWER, UPPER>(m, i, r0, r1, s1, Ap.at(), Dp.at(), inp.at(), outp.at());
+  ilu_colour_row<T, LOWER, UPPER>(m, i, r0, r1, s1, sat<BATCH>(Ap), sat<BATCH>(Dp),
+                                  sat<BATCH>(inp), sat<BATCH>(outp));
 }
 
 template <bool LOWER, bool UPPER, bool COH = false>
@@ -155,15 +165,16 @@ __device__ __forceinline__ void ilu_colour_packed_row(
 
 // ilu_colour_kernel with packed factors: L / U blocks in H slots 0..3 (local faces 0..3),
 // inv(U_ii) in D (one slot)
-template <bool LOWER, bool UPPER>
+template <bool LOWER, bool UPPER, bool BATCH>
 __global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
     DevMesh m, int r0, int r1, int s1, SlotPtr<const __half2> Hp, SlotPtr<const float> HSp,
     SlotPtr<const __half2> Dp, SlotPtr<const float> DSp, SlotPtr<const float> inp,
     SlotPtr<float> outp, const int32_t* run) {
   const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= r1 || slot_idle(run)) return;
-  ilu_colour_packed_row<LOWER, UPPER>(m, i, r0, r1, s1, Hp.at(), HSp.at(), Dp.at(), DSp.at(),
-                                      inp.at(), outp.at());
+  ilu_colour_packed_row<LOWER, UPPER>(m, i, r0, r1, s1, sat<BATCH>(Hp), sat<BATCH>(HSp),
+                                      sat<BATCH>(Dp), sat<BATCH>(DSp), sat<BATCH>(inp),
+                                      sat<BATCH>(outp));
 }
 
 // ---- persistent colour sweep ----------------------------------------------------------------
@@ -418,17 +429,17 @@ static __global__ void __launch_bounds__(256) jacobi_apply_packed_kernel(
 // ---- matrix-vector products ------------------------------------------------------------------
 
 // y = A x (ELL), or y = b - A x when b is given
-template <class T>
+template <class T, bool BATCH>
 __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, SlotPtr<const T> Ap,
                                                    SlotPtr<const T> xp, SlotPtr<const T> bp,
                                                    SlotPtr<T> yp, const int32_t* run) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nc = m.nc;
   if (i >= nc || slot_idle(run)) return;
-  const T* __restrict__ A = Ap.at();
-  const T* __restrict__ x = xp.at();
-  const T* __restrict__ b = bp.p ? bp.at() : nullptr;
-  T* __restrict__ y = yp.at();
+  const T* __restrict__ A = sat<BATCH>(Ap);
+  const T* __restrict__ x = sat<BATCH>(xp);
+  const T* __restrict__ b = bp.p ? sat<BATCH>(bp) : nullptr;
+  T* __restrict__ y = sat<BATCH>(yp);
   T acc[5], xi[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)i * 5 + v];
@@ -457,17 +468,18 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, SlotPtr<const T> A
 
 // y = A x (or b - A x) with A in packed form: per block, the neighbour's values are scaled
 // by the block's scale and multiplied by the 16-bit entries
-static __global__ void __launch_bounds__(256) spmv_packed_kernel(
+template <bool BATCH>
+__global__ void __launch_bounds__(256) spmv_packed_kernel(
     DevMesh m, SlotPtr<const __half2> Hp, SlotPtr<const float> Sp, SlotPtr<const float> xp,
     SlotPtr<const float> bp, SlotPtr<float> yp, const int32_t* run) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int nc = m.nc;
   if (i >= nc || slot_idle(run)) return;
-  const __half2* __restrict__ H = Hp.at();
-  const float* __restrict__ S = Sp.at();
-  const float* __restrict__ x = xp.at();
-  const float* __restrict__ b = bp.p ? bp.at() : nullptr;
-  float* __restrict__ y = yp.at();
+  const __half2* __restrict__ H = sat<BATCH>(Hp);
+  const float* __restrict__ S = sat<BATCH>(Sp);
+  const float* __restrict__ x = sat<BATCH>(xp);
+  const float* __restrict__ b = bp.p ? sat<BATCH>(bp) : nullptr;
+  float* __restrict__ y = sat<BATCH>(yp);
   float acc[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
   // branch-free, so that every slot's loads can be in flight together: the block of a slot
   // without a neighbour is zero (boundary face, or the empty fourth slot of a triangle), and
