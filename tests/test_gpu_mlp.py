@@ -35,7 +35,10 @@ def _blocks(v):
     return out
 
 
-def test_gradient_matches_oracle():
+@pytest.mark.parametrize("B", [256, 1024])
+def test_gradient_matches_oracle(B):
+    """B = 1024 also takes the split-K path of the weight-gradient GEMM (two partials of 512
+    rows reduced in a fixed order)."""
     mesh = meshgen.bump_channel(12, 4, 4, 0.08)
     ctx = _ctx(mesh)
     net = lib.WarmStart(ctx, seed=3)
@@ -48,7 +51,6 @@ def test_gradient_matches_oracle():
         blocks[f"b{l}"][:] = rng.normal(size=blocks[f"b{l}"].size) * 0.05
     p = np.concatenate([blocks[n] for n, _ in M.layout()]).astype(np.float32)
     net.set_params(p)
-    B = 256
     cells = rng.integers(0, ctx.n_cells, B)
     cond = rng.normal(size=(B, 3))
     tgt = rng.normal(size=(B, 5)) * 0.5
