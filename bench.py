@@ -875,7 +875,10 @@ def run_isweep(args, wl, torch, mesh, clocks):
         qd = 0.5 * float(np.sum(machs[q] ** 2))  # dynamic pressure (rho = 1, A_ref = 1)
         rows.append(dict(mach=[float(x) for x in machs[q]],
                          plain_steps=int(p["steps"][q]), plain_seconds=float(p["seconds"][q]),
-                         plain_converged=bool(conv_p[q]), batched_steps=int(b["steps"][q]),
+                         plain_converged=bool(conv_p[q]),
+                         plain_final_drop=float(p["final_res"][q]),
+                         batched_final_drop=float(b["final_res"][q]),
+                         batched_steps=int(b["steps"][q]),
                          batched_converged=bool(conv_b[q]),
                          force_coefficient_abs_diff=float(np.abs(b["force"][q] - p["force"][q]).max() / qd)))
     both = [r for r in rows if r["plain_converged"] and r["batched_converged"]]
@@ -897,6 +900,7 @@ def run_isweep(args, wl, torch, mesh, clocks):
                               "plain_fp64": int(conv_p.sum()), "plain_of": nplain},
                 "seconds": {"batched_fp32_system": t_batch, "plain_fp64": t_plain},
                 "batched_steps_per_condition": [int(x) for x in b["steps"]],
+                "batched_final_drop_per_condition": [float(x) for x in b["final_res"]],
                 "host_syncs": s1["host_syncs"] - s0["host_syncs"],
                 "tuning": tuning,
                 "max_force_coefficient_abs_diff": (max(r["force_coefficient_abs_diff"] for r in both)
