@@ -114,8 +114,9 @@ WORKLOADS = {
     # absolute residual (1e-8 x the freestream state's residual), and the plain FP64 solver on
     # the first plain_sample of them for the reference answer
     "production_gauss_648k": dict(kind="production", mesh=("gauss", 60, 30, 60, 1.05),
-                                  train=(1, 512), test=(2, 64), plain_sample=8, slots=32,
-                                  data_max_steps=200, max_steps=300, train_steps=20000,
+                                  train=(1, 512), test=(2, 64), plain_sample=4, slots=32,
+                                  data_max_steps=150, data_budget_s=1200.0, max_steps=200,
+                                  train_steps=20000,
                                   batch=8192, prod_tol=0.1,
                                   opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
                                             linear_solver=1, linear_solver_tol=1e-2,
@@ -711,22 +712,38 @@ def run_production(args, wl, torch, mesh, clocks):
     train, test = machs(*wl["train"]), machs(*wl["test"])
     slots = min(wl["slots"], len(train))
     clocks.start()
-    # 1. training data: the batched sweep from the freestream to a 1e-8 drop
+    # 1. training data: the batched sweep from the freestream to a 1e-8 drop, in chunks of
+    # two slot-fills; no new chunk starts after data_budget_s seconds (progress on stderr)
     t0 = time.perf_counter()
     cd = lib.Context(mesh, lib.default_options(**op), machs=train[:slots])
     nc = cd.n_cells
-    d = cd.implicit_sweep(train, drop=1e-8, max_steps=wl["data_max_steps"], states=True)
+    chunk = 2 * slots
+    states, ok_machs, attempted, data_steps = [], [], 0, 0
+    for c0 in range(0, len(train), chunk):
+        part = train[c0:c0 + chunk]
+        d = cd.implicit_sweep(part, drop=1e-8, max_steps=wl["data_max_steps"], states=True)
+        conv = d["final_res"] <= 1e-8
+        states.extend(d["U"][conv])
+        ok_machs.extend(part[conv])
+        attempted += len(part)
+        data_steps += int(d["steps"].sum())
+        del d
+        el = time.perf_counter() - t0
+        print(json.dumps({"progress": "training data", "attempted": attempted,
+                          "converged": len(ok_machs), "seconds": el}), file=sys.stderr,
+              flush=True)
+        if el > wl.get("data_budget_s", 1e30):
+            break
     cd.close()
     t_data = time.perf_counter() - t0
-    ok = d["final_res"] <= 1e-8
-    states = d["U"][ok]
-    del d["U"]
+    states = np.array(states)
+    ok_machs = np.array(ok_machs)
     # 2. training on the GPU (tcgen05 GEMMs, AdamW)
     base = lib.Context(mesh, lib.default_options(**op))
     net = lib.WarmStart(base, seed=0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    loss = net.train(train[ok], states, steps=wl["train_steps"], batch=wl["batch"], lr=1e-3,
+    loss = net.train(ok_machs, states, steps=wl["train_steps"], batch=wl["batch"], lr=1e-3,
                      weight_decay=1e-4, seed=1)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
@@ -749,6 +766,8 @@ def run_production(args, wl, torch, mesh, clocks):
     cold = cc.implicit_sweep(test, target=target, max_steps=wl["max_steps"], states=True)
     cc.close()
     t_cold = time.perf_counter() - t0
+    print(json.dumps({"progress": "cold", "converged": int((cold["final_res"] * r0 <= target).sum()),
+                      "seconds": t_cold}), file=sys.stderr, flush=True)
     # from a predicted field the CFL ramp starts at 100 (10 steps to 1000)
     ow = dict(op, cfl_ramp_start=100.0, cfl_ramp_steps=10)
     t0 = time.perf_counter()
@@ -756,6 +775,10 @@ def run_production(args, wl, torch, mesh, clocks):
     warm = cw.implicit_sweep(test, U0=U0, target=target, max_steps=wl["max_steps"], states=True)
     cw.close()
     t_warm = time.perf_counter() - t0
+    print(json.dumps({"progress": "warm", "converged": int((warm["final_res"] * r0 <= target).sum()),
+                      "seconds": t_warm, "steps_mean": float(warm["steps"].mean()),
+                      "cold_steps_mean": float(cold["steps"].mean())}), file=sys.stderr,
+          flush=True)
     # the plain FP64 solver, one condition per context, on a sample
     npl = min(n, wl["plain_sample"])
     t0 = time.perf_counter()
@@ -802,7 +825,8 @@ def run_production(args, wl, torch, mesh, clocks):
                      "update; network bf16 GEMMs (tcgen05) with fp32 accumulation",
             "data": "synthetic",
             "config": {"workload": args.workload, "cells": nc, "slots": ns,
-                       "train_conditions": len(train), "train_converged": int(ok.sum()),
+                       "train_conditions": len(train), "train_attempted": attempted,
+                       "train_converged": len(ok_machs), "train_data_steps": data_steps,
                        "test_conditions": n, "plain_sample": npl,
                        "train_steps": wl["train_steps"], "batch": wl["batch"],
                        "production_linear_tol": wl["prod_tol"], "parallelism": "replicas1",
