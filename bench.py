@@ -534,6 +534,13 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
                          prof_steps=0)
     ctx64.close()
     prec = int(wl["opts"].get("precision", 0))
+    fp32 = None
+    if prec == 2:
+        # the FP32 system stored in FP32 (precision 1) on the same steps
+        c32 = lib.Context(mesh, lib.default_options(**dict(wl["opts"], precision=1)))
+        fp32 = implicit_leg(args, torch, c32, args.steps, args.warmup, flush, with_e2e=False,
+                            prof_steps=0)
+        c32.close()
     prof = mixed["prof"]
     cats = {"precond": BYTES_PRECOND[prec] * nc, "spmv": BYTES_SPMV[prec] * nc}
     dom = max(cats, key=lambda k: prof[k][0])
@@ -580,9 +587,47 @@ def run_implicit(args, wl, torch, ctx, mesh, world, rank, local_rank, dist):
                          "category_ms_per_step": {k: v[0] / mixed["prof_steps"]
                                                   for k, v in prof.items()}},
             "clocks": clk}
+    if fp32 is not None:
+        line["fp32_storage"] = {"value": world * nc * args.steps / (fp32["ms"] / 1e3),
+                                "ms_per_step": fp32["ms"] / args.steps,
+                                "linear_iterations_per_step": float(fp32["hist"][:, 12].mean()),
+                                "state_rel_l2_vs_fp64": float(
+                                    np.linalg.norm(fp32["state"] - plain["state"])
+                                    / np.linalg.norm(plain["state"]))}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = implicit_cpu_baseline(wl, mesh)
+        line["error_vs_fp64_oracle"] = oracle_error(wl, mesh, lib)
     return line
+
+
+def oracle_error(wl, mesh, lib, steps: int = 2):
+    """The GPU's FP64 system and the production form against the FP64 oracle (the CPU
+    restatement given the GPU's block-ILU(0) order) over the first `steps` implicit steps
+    from the freestream on the workload's own mesh."""
+    from oracle import pyoracle
+    o = wl["opts"]
+    out = {"steps": steps}
+    states = {}
+    for name, prec in (("fp64_system", 0), ("production", int(o.get("precision", 0)))):
+        c = lib.Context(mesh, lib.default_options(**dict(o, precision=prec)))
+        h = c.implicit_steps(steps)
+        states[name] = (c.get_state(), h)
+        order = c.ilu_order()
+        c.close()
+    O = pyoracle.Oracle(mesh, solver=1, local_dt=o["local_time_step"], cfl=o["courant_num"],
+                        mach=o.get("freestream_mach", (0.84, 0.0, 0.0)), lin_precond=1,
+                        lin_tol=o["linear_solver_tol"], lin_maxiter=o["linear_solver_max_iter"],
+                        lin_restart=o["gmres_restart"], ramp_steps=o["cfl_ramp_steps"],
+                        ramp_cfl0=o["cfl_ramp_start"], ramp_cfl1=o["cfl_ramp_end"],
+                        threads=os.cpu_count() or 1)
+    O.set_ilu_order(order)
+    ho = O.implicit_run(steps)
+    Uo = O.get_state()
+    for name, (U, h) in states.items():
+        out[name] = {"state_rel_l2": float(np.linalg.norm(U - Uo) / np.linalg.norm(Uo)),
+                     "state_max_rel": float(np.abs(U - Uo).max() / np.abs(Uo).max()),
+                     "linear_iterations_equal": bool(np.array_equal(h[:, 12], ho[:, 12]))}
+    return out
 
 
 def run_warmstart(args, wl, torch, mesh, clocks):
