@@ -30,7 +30,8 @@ EXPORTED = [
     "bes_output_default", "bes_output_from_besi", "bes_write", "bes_write_host", "bes_solve",
     "bes_create_batch", "bes_conditions", "bes_set_active", "bes_sweep_run",
     "bes_implicit_stats", "bes_set_linear_guard", "bes_set_condition", "bes_implicit_sweep",
-    "bes_tuning", "bes_fp64_fma_rate", "bes_host_layout_digest",
+    "bes_tuning", "bes_fp64_fma_rate", "bes_host_layout_digest", "bes_checkpoint_save",
+    "bes_checkpoint_load",
     "bes_mlp_create", "bes_mlp_destroy", "bes_mlp_last_error", "bes_mlp_train", "bes_mlp_infer",
     "bes_mlp_init_state", "bes_mlp_params", "bes_mlp_features", "bes_mlp_loss_grad",
     "bes_mlp_apply_grad", "bes_mlp_normalisation",
@@ -144,6 +145,8 @@ def load(path: str = LIB_PATH):
     L.bes_set_linear_guard.argtypes = [P, ctypes.c_int32]
     L.bes_tuning.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
     L.bes_fp64_fma_rate.argtypes = [D]
+    L.bes_checkpoint_save.argtypes = [P, ctypes.c_char_p]
+    L.bes_checkpoint_load.argtypes = [P, ctypes.c_char_p]
     L.bes_host_layout_digest.argtypes = [ctypes.POINTER(MeshArrays), ctypes.c_int32,
                                          ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
                                          ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
@@ -501,6 +504,14 @@ class Context:
         self._check(load().bes_implicit_stats(self.h, _i(out)))
         return dict(steps=int(out[0]), host_syncs=int(out[1]), arnoldi_steps=int(out[2]),
                     restart_cycles=int(out[3]))
+
+    def checkpoint_save(self, path: str):
+        """bes_checkpoint_save: state, controllers and counters to a binary file."""
+        self._check(load().bes_checkpoint_save(self.h, path.encode()))
+
+    def checkpoint_load(self, path: str):
+        """bes_checkpoint_load: continue from a checkpoint of a context like this one."""
+        self._check(load().bes_checkpoint_load(self.h, path.encode()))
 
     def tuning(self) -> str:
         """bes_tuning: the autotuner's candidates, their device times and its choices."""

@@ -393,6 +393,16 @@ int bes_write_host(const bes_mesh_arrays* mesh, const bes_options* opt, const do
  * (OUTPUT_SLIP_WALL) slip_wall_<step>.csv are written after the steps save_interval selects. */
 int bes_solve(bes_ctx* ctx, const bes_output* out);
 
+/* Checkpoint and resume (no counterpart in the reference, which has no restart reader and
+ * writes output snapshots only, src/SolverExplicit.cpp:427-433).  save writes the FP64 state of
+ * every condition, each condition's freestream, active flag, CFL controller and step counters,
+ * and the explicit step counter to a binary file; load restores them into a context created
+ * with the same mesh, solver type and condition count, which then continues bit for bit as
+ * the saved one would have.  BES_ERR_INVALID (with a message) for an unreadable or
+ * mismatched file. */
+int bes_checkpoint_save(bes_ctx* ctx, const char* path);
+int bes_checkpoint_load(bes_ctx* ctx, const char* path);
+
 /* Sizes of the ABI structs as compiled: out[0] = sizeof(bes_options),
  * out[1] = sizeof(bes_mesh_arrays), out[2] = sizeof(bes_output).  out [3].  Lets a binding
  * check its struct mirrors. */
