@@ -207,8 +207,9 @@ extern "C" int bes_options_from_besi(const char* path, bes_options* o, char* mes
       o->cfl_ramp_start = a;
       o->cfl_ramp_end = b;
     } else if (key == "SWEEP_KERNEL") {  // additive
-      const int w = word({"AUTO", "PER_COLOUR", "PERSISTENT"});
-      if (w < 0) return bad("SWEEP_KERNEL must be AUTO, PER_COLOUR or PERSISTENT");
+      const int w = word({"AUTO", "PER_COLOUR", "PERSISTENT", "PER_COLOUR_LOADS_FIRST"});
+      if (w < 0)
+        return bad("SWEEP_KERNEL must be AUTO, PER_COLOUR, PERSISTENT or PER_COLOUR_LOADS_FIRST");
       o->sweep_kernel = w;
     } else if (key == "JACOBIAN_REPEAT") {  // additive: 5 reproduces the reference
       if (!num(0, x) || x < 1) return bad("JACOBIAN_REPEAT must be >= 1");

@@ -275,8 +275,15 @@ void enqueue_precond(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> in, co
           auto HS = cslots((const float*)S.LUs, 4LL * S.nc);
           auto D = cslots((const __half2*)S.D16, 13LL * S.nc);
           auto DS = cslots((const float*)S.Ds, (int64_t)S.nc);
-#define BES_PACKED_SWEEP(LO, UP, BA) \
-  ilu_colour_packed_kernel<LO, UP, BA><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, in, Z, run)
+#define BES_PACKED_SWEEP(LO, UP, BA)                                                          \
+  do {                                                                                        \
+    if (c->imp.sweep_kernel == 3)                                                             \
+      ilu_colour_packed_ld_kernel<LO, UP, BA><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS, \
+                                                                   in, Z, run);               \
+    else                                                                                      \
+      ilu_colour_packed_kernel<LO, UP, BA><<<grid, 128, 0, s>>>(m, r0, r1, s1, H, HS, D, DS,   \
+                                                                in, Z, run);                  \
+  } while (0)
           if (S.nslot > 1) {
             if (lower && !upper) BES_PACKED_SWEEP(true, false, true);
             else if (lower) BES_PACKED_SWEEP(true, true, true);
@@ -556,10 +563,14 @@ int tune_sweep(bes_ctx* c) {
   }
   SweepPlan plan;
   const bool can_persist = sweep_plan(c->soa, plan) && I.persistent_blocks > 0;
-  if (c->opt.sweep_kernel == 1 || c->opt.sweep_kernel == 2) {
-    I.sweep_kernel = (c->opt.sweep_kernel == 2 && can_persist) ? 2 : 1;
+  static const char* kNames[4] = {"", "one launch per colour", "persistent",
+                                  "one launch per colour, loads first"};
+  if (c->opt.sweep_kernel >= 1 && c->opt.sweep_kernel <= 3) {
+    I.sweep_kernel = c->opt.sweep_kernel;
+    if (I.sweep_kernel == 2 && !can_persist) I.sweep_kernel = 1;
+    if (I.sweep_kernel == 3 && !I.packed) I.sweep_kernel = 1;
     std::snprintf(line, sizeof(line), "colour sweep: %s (fixed by the options)\n",
-                  I.sweep_kernel == 2 ? "persistent" : "one launch per colour");
+                  kNames[I.sweep_kernel]);
     I.tuning += line;
     return BES_OK;
   }
@@ -569,11 +580,12 @@ int tune_sweep(bes_ctx* c) {
   double best = 1e300;
   int choice = 1;
   std::string rep = "colour sweep:";
-  for (int cand = 1; cand <= 2; ++cand) {
+  for (int cand = 1; cand <= 3; ++cand) {
     if (cand == 2 && !can_persist) {
       rep += " persistent not possible;";
       continue;
     }
+    if (cand == 3 && !I.packed) continue;  // a form of the 16-bit storage only
     I.sweep_kernel = cand;
     bool ok = true;
     float ms = 0.0f;
@@ -608,6 +620,8 @@ int tune_sweep(bes_ctx* c) {
     const double per = ms / 10.0;
     if (cand == 1)
       std::snprintf(line, sizeof(line), " one launch per colour %.4f ms;", per);
+    else if (cand == 3)
+      std::snprintf(line, sizeof(line), " one launch per colour, loads first %.4f ms;", per);
     else if (ok)
       std::snprintf(line, sizeof(line), " persistent (%d blocks of 128) %.4f ms;",
                     I.persistent_blocks, per);
@@ -622,8 +636,8 @@ int tune_sweep(bes_ctx* c) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   I.sweep_kernel = choice;
-  std::snprintf(line, sizeof(line), " taken: %s (%d slots, %d cells)\n",
-                choice == 2 ? "persistent" : "one launch per colour", S.nslot, S.nc);
+  std::snprintf(line, sizeof(line), " taken: %s (%d slots, %d cells)\n", kNames[choice],
+                S.nslot, S.nc);
   rep += line;
   I.tuning += rep;
   return BES_OK;

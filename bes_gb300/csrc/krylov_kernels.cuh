@@ -177,6 +177,88 @@ __global__ void __launch_bounds__(128) ilu_colour_packed_kernel(
                                       sat<BATCH>(outp));
 }
 
+// The packed colour sweep with every qualifying slot's loads (scale, 16-bit block, the
+// neighbour's values) issued before any arithmetic: two dependent round trips per row
+// (neighbour ids, then everything else) instead of one per qualifying slot, at the cost of
+// registers.  The arithmetic is that of ilu_colour_packed_row in the same order, so the
+// results are identical; the autotuner keeps it only where it is faster.
+template <bool LOWER, bool UPPER>
+__device__ __forceinline__ void ilu_colour_packed_row_ld(
+    const DevMesh& m, int i, int r0, int r1, int s1, const __half2* __restrict__ H,
+    const float* __restrict__ HS, const __half2* __restrict__ D, const float* __restrict__ DS,
+    const float* __restrict__ in, float* __restrict__ out) {
+  const int nc = m.nc;
+  const float* own = (LOWER || r0 == 0) ? in : out;
+  int jn[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) jn[s] = m.adj[s * nc + i];
+  float acc[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
+  bool q[4];
+  __half2 hb[4][13];
+  float sc[4], y[4][5];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int j = jn[s];
+    const bool lower = LOWER && j >= 0 && j < r0;
+    const bool upper = UPPER && j >= r1;
+    q[s] = lower || upper;
+    if (q[s]) {
+      const float* src = (lower && j < s1) ? in : out;
+      sc[s] = HS[(int64_t)s * nc + i];
+#pragma unroll
+      for (int p = 0; p < 13; ++p) hb[s][p] = H[(int64_t)(s * 13 + p) * nc + i];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) y[s][v] = src[(int64_t)j * 5 + v];
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    if (!q[s]) continue;
+    float a[26], ys[5];
+#pragma unroll
+    for (int p = 0; p < 13; ++p) {
+      const float2 f = __half22float2(hb[s][p]);
+      a[2 * p] = f.x;
+      a[2 * p + 1] = f.y;
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) ys[v] = sc[s] * y[s][v];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) acc[r] = fmaf(-a[r * 5 + c], ys[c], acc[r]);
+  }
+  if (UPPER) {
+    float a[26];
+    load_packed(D, 0, nc, i, a);
+    const float d = DS[i];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      float x = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) x = fmaf(a[r * 5 + c], acc[c], x);
+      out[(int64_t)i * 5 + r] = d * x;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[(int64_t)i * 5 + v] = acc[v];
+  }
+}
+
+template <bool LOWER, bool UPPER, bool BATCH>
+__global__ void __launch_bounds__(128) ilu_colour_packed_ld_kernel(
+    DevMesh m, int r0, int r1, int s1, SlotPtr<const __half2> Hp, SlotPtr<const float> HSp,
+    SlotPtr<const __half2> Dp, SlotPtr<const float> DSp, SlotPtr<const float> inp,
+    SlotPtr<float> outp, const int32_t* run) {
+  const int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1 || slot_idle(run)) return;
+  ilu_colour_packed_row_ld<LOWER, UPPER>(m, i, r0, r1, s1, sat<BATCH>(Hp), sat<BATCH>(HSp),
+                                         sat<BATCH>(Dp), sat<BATCH>(DSp), sat<BATCH>(inp),
+                                         sat<BATCH>(outp));
+}
+
 // ---- persistent colour sweep ----------------------------------------------------------------
 // One launch per preconditioner application: a grid of resident blocks (cooperative launch,
 // sized by occupancy) walks the 2C-1 colour stages of the sweep in order, the rows of every

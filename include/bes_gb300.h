@@ -90,7 +90,8 @@ typedef struct {
   int32_t sweep_kernel;           /* SWEEP_KERNEL (additive): block-ILU(0) colour sweeps as
                                      0 the autotuner's choice (timed on the first step's
                                      system, see bes_tuning), 1 one launch per colour, 2 one
-                                     persistent launch per sweep */
+                                     persistent launch per sweep, 3 one launch per colour
+                                     with every load of a row issued first (precision 2) */
   int32_t reserved_i;
   double reserved[2];
 } bes_options;

@@ -153,14 +153,15 @@ def test_sweep_queue_through_slots_matches_single_solves(precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1, 2])
-def test_persistent_colour_sweep_matches_per_colour_launches(precision):
-    """SWEEP_KERNEL 2 (one persistent launch per sweep, grid barrier between colours) computes
-    each row exactly as the per-colour launches (SWEEP_KERNEL 1): identical steps, single and
+def test_colour_sweep_forms_give_identical_steps(precision):
+    """SWEEP_KERNEL 2 (one persistent launch per sweep, grid barrier between colours) and 3
+    (one launch per colour, every load of a row issued first; the 16-bit storage) compute each
+    row exactly as the per-colour launches (SWEEP_KERNEL 1): identical steps, single and
     batched."""
     nbuild.build()
     mesh = meshgen.bump_channel(24, 8, 6, 0.08)
     runs = {}
-    for kern in (1, 2):
+    for kern in (1, 2, 3):
         one = lib.Context(mesh, _opts(freestream_mach=MACHS[0], precision=precision,
                                       sweep_kernel=kern))
         bat = lib.Context(mesh, _opts(precision=precision, sweep_kernel=kern), machs=MACHS)
@@ -168,12 +169,16 @@ def test_persistent_colour_sweep_matches_per_colour_launches(precision):
                       bat.get_state(), one.tuning())
         one.close()
         bat.close()
-    rep = runs[2][4]
-    assert "fixed by the options" in rep
-    if rep.startswith("colour sweep: one launch") or "could not be captured" in rep:
-        pytest.skip("the persistent sweep is not available here: " + rep)
-    for a, b in zip(runs[1][:4], runs[2][:4]):
-        assert np.array_equal(a, b)
+    for kern in (2, 3):
+        rep = runs[kern][4]
+        assert "fixed by the options" in rep
+        if kern == 2 and (rep.startswith("colour sweep: one launch")
+                          or "could not be captured" in rep):
+            continue  # the persistent sweep is not available on this device
+        if kern == 3:
+            assert ("loads first" in rep) == (precision == 2)
+        for a, b in zip(runs[1][:4], runs[kern][:4]):
+            assert np.array_equal(a, b)
 
 
 def test_autotuner_reports_its_choice():
