@@ -164,7 +164,7 @@ struct ImplicitBuffers {
   // colour sweeps: one launch per colour, or one persistent launch per sweep (grid of
   // resident blocks with a bounded grid barrier between colours); chosen by the autotuner on
   // the first step unless the options fix it
-  int sweep_kernel = 1;        // 1 per colour, 2 persistent
+  int sweep_kernel = 1;        // 1 per colour, 2 persistent, 3 per colour with loads first
   bool tuned = false;
   int persistent_blocks = 0;   // grid of the persistent sweep
   unsigned int* sync_count = nullptr;  // grid barrier: arrivals, generation, error flag

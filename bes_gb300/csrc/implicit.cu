@@ -49,7 +49,9 @@ int imp_malloc(bes_ctx* c, void** p, size_t bytes) {
   return BES_OK;
 }
 
-inline int64_t basis_stride(int64_t nc) { return (5 * nc + 63) / 64 * 64; }
+// Stride of the Krylov vectors of a slot: 5 nc values, at least four more (the two-chunk
+// gathers of the last cell read up to three values past it), rounded up to 64 values.
+inline int64_t basis_stride(int64_t nc) { return (5 * nc + 4 + 63) / 64 * 64; }
 
 inline bool uses_ilu(const bes_ctx* c) { return c->opt.linear_solver == 1 || c->opt.linear_solver == 2; }
 
@@ -612,16 +614,17 @@ int tune_sweep(bes_ctx* c) {
         if (err) ok = false;
       }
     }
-    cudaGetLastError();  // a refused cooperative launch leaves no sticky error
+    // a refused launch leaves no sticky error; its form is dropped
+    if (cudaGetLastError() != cudaSuccess) ok = false;
     if (cand == 2) {
       const int rc = reset_grid_sync(c);
       if (rc) return rc;
     }
     const double per = ms / 10.0;
-    if (cand == 1)
-      std::snprintf(line, sizeof(line), " one launch per colour %.4f ms;", per);
-    else if (cand == 3)
-      std::snprintf(line, sizeof(line), " one launch per colour, loads first %.4f ms;", per);
+    if (cand != 2 && ok)
+      std::snprintf(line, sizeof(line), " %s %.4f ms;", kNames[cand], per);
+    else if (cand != 2)
+      std::snprintf(line, sizeof(line), " %s failed;", kNames[cand]);
     else if (ok)
       std::snprintf(line, sizeof(line), " persistent (%d blocks of 128) %.4f ms;",
                     I.persistent_blocks, per);

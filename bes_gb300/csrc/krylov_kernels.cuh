@@ -46,6 +46,68 @@ __device__ __forceinline__ bool slot_idle(const int32_t* run) {
   return run != nullptr && run[blockIdx.y] == 0;
 }
 
+// ---- matrix words read once per application --------------------------------------------------
+// The packed matrix and factor words are read once per SpMV or preconditioner application, and
+// their stream is several times larger than L2.  Under the default policy it evicts the Krylov
+// vectors whose values the neighbour gathers read again, and every gathered neighbour costs a
+// DRAM sector: the 2.16M-cell SpMV read 829 MB from DRAM against 696 MB of compulsory traffic.
+// Loaded with an evict_first policy the matrix words leave the vectors in L2 (696 MB).
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ __half2 ld_once(const __half2* a, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return *reinterpret_cast<const __half2*>(&v);
+}
+__device__ __forceinline__ float ld_once(const float* a, uint64_t pol) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint4 ld_once(const uint4* a, uint64_t pol) {
+  uint4 v;
+  asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+      : "l"(a), "l"(pol));
+  return v;
+}
+// load_packed with the evict_first policy
+__device__ __forceinline__ void load_packed_once(const __half2* __restrict__ H, int s, int nc, int i,
+                                                 float* a, uint64_t pol) {
+#pragma unroll
+  for (int p = 0; p < 13; ++p) {
+    const float2 f = __half22float2(ld_once(H + (int64_t)(s * 13 + p) * nc + i, pol));
+    a[2 * p] = f.x;
+    a[2 * p + 1] = f.y;
+  }
+}
+
+// ---- gathers of a cell's five values ------------------------------------------------------------
+// A Krylov vector holds a cell's five FP32 values in 20 consecutive bytes, which always lie in
+// two aligned 16-byte chunks.  Loading those two chunks takes two load instructions per
+// neighbour instead of five (for a warp whose neighbours are scattered, one L1 wavefront per
+// lane and instruction).  The vectors are 16-byte aligned and have at least 16 bytes after the
+// last cell of every slot (the vector stride), so both chunks are in bounds.  The values are
+// the same floats either way.
+__device__ __forceinline__ void gather5(const float* __restrict__ x, int j, float* y) {
+  const int64_t e0 = (int64_t)j * 5;
+  const float4* p = reinterpret_cast<const float4*>(x) + (e0 >> 2);
+  const float4 a = p[0], b = p[1];
+  const float w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  const int o = (int)(e0 & 3);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    float t = w[v];
+    t = o == 1 ? w[v + 1] : t;
+    t = o == 2 ? w[v + 2] : t;
+    t = o == 3 ? w[v + 3] : t;
+    y[v] = t;
+  }
+}
+
 // ---- preconditioners ------------------------------------------------------------------------
 
 // Load of a Krylov vector entry; COH: through L2 only (ld.global.cg), for values that other
@@ -71,10 +133,15 @@ __device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, 
                                                const T* __restrict__ Dinv,
                                                const T* __restrict__ in, T* __restrict__ out) {
   const int nc = m.nc;
+  constexpr bool G = !COH && std::is_same<T, float>::value;  // two-chunk gathers
   const T* own = (LOWER || r0 == 0) ? in : out;
   T acc[5];
+  if constexpr (G) {
+    gather5(own, i, acc);
+  } else {
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = vld<COH>(own + (int64_t)i * 5 + v);
+    for (int v = 0; v < 5; ++v) acc[v] = vld<COH>(own + (int64_t)i * 5 + v);
+  }
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     const int j = m.adj[s * nc + i];
@@ -83,8 +150,12 @@ __device__ __forceinline__ void ilu_colour_row(const DevMesh& m, int i, int r0, 
     if (!lower && !upper) continue;
     const T* src = (lower && j < s1) ? in : out;
     T y[5];
+    if constexpr (G) {
+      gather5(src, j, y);
+    } else {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) y[v] = vld<COH>(src + (int64_t)j * 5 + v);
+      for (int v = 0; v < 5; ++v) y[v] = vld<COH>(src + (int64_t)j * 5 + v);
+    }
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -121,10 +192,15 @@ __device__ __forceinline__ void ilu_colour_packed_row(
     const float* __restrict__ HS, const __half2* __restrict__ D, const float* __restrict__ DS,
     const float* __restrict__ in, float* __restrict__ out) {
   const int nc = m.nc;
+  const uint64_t pol = l2_evict_first();
   const float* own = (LOWER || r0 == 0) ? in : out;
   float acc[5];
+  if constexpr (!COH) {
+    gather5(own, i, acc);
+  } else {
 #pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = vld<COH>(own + (int64_t)i * 5 + v);
+    for (int v = 0; v < 5; ++v) acc[v] = vld<COH>(own + (int64_t)i * 5 + v);
+  }
   // the four neighbour ids first (one round trip), then the qualifying slots
   int jn[4];
 #pragma unroll
@@ -136,11 +212,17 @@ __device__ __forceinline__ void ilu_colour_packed_row(
     const bool upper = UPPER && j >= r1;
     if (!lower && !upper) continue;
     const float* src = (lower && j < s1) ? in : out;
-    const float sc = HS[(int64_t)s * nc + i];
+    const float sc = ld_once(HS + (int64_t)s * nc + i, pol);
     float y[5], a[26];
+    if constexpr (!COH) {
+      gather5(src, j, y);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) y[v] = sc * vld<COH>(src + (int64_t)j * 5 + v);
-    load_packed(H, s, nc, i, a);
+      for (int v = 0; v < 5; ++v) y[v] *= sc;
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) y[v] = sc * vld<COH>(src + (int64_t)j * 5 + v);
+    }
+    load_packed_once(H, s, nc, i, a, pol);
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -148,8 +230,8 @@ __device__ __forceinline__ void ilu_colour_packed_row(
   }
   if (UPPER) {
     float a[26];
-    load_packed(D, 0, nc, i, a);
-    const float sc = DS[i];
+    load_packed_once(D, 0, nc, i, a, pol);
+    const float sc = ld_once(DS + i, pol);
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       float x = 0.0f;
@@ -188,13 +270,13 @@ __device__ __forceinline__ void ilu_colour_packed_row_ld(
     const float* __restrict__ HS, const __half2* __restrict__ D, const float* __restrict__ DS,
     const float* __restrict__ in, float* __restrict__ out) {
   const int nc = m.nc;
+  const uint64_t pol = l2_evict_first();
   const float* own = (LOWER || r0 == 0) ? in : out;
   int jn[4];
 #pragma unroll
   for (int s = 0; s < 4; ++s) jn[s] = m.adj[s * nc + i];
   float acc[5];
-#pragma unroll
-  for (int v = 0; v < 5; ++v) acc[v] = own[(int64_t)i * 5 + v];
+  gather5(own, i, acc);
   bool q[4];
   __half2 hb[4][13];
   float sc[4], y[4][5];
@@ -206,11 +288,10 @@ __device__ __forceinline__ void ilu_colour_packed_row_ld(
     q[s] = lower || upper;
     if (q[s]) {
       const float* src = (lower && j < s1) ? in : out;
-      sc[s] = HS[(int64_t)s * nc + i];
+      sc[s] = ld_once(HS + (int64_t)s * nc + i, pol);
 #pragma unroll
-      for (int p = 0; p < 13; ++p) hb[s][p] = H[(int64_t)(s * 13 + p) * nc + i];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) y[s][v] = src[(int64_t)j * 5 + v];
+      for (int p = 0; p < 13; ++p) hb[s][p] = ld_once(H + (int64_t)(s * 13 + p) * nc + i, pol);
+      gather5(src, j, y[s]);
     }
   }
 #pragma unroll
@@ -232,8 +313,8 @@ __device__ __forceinline__ void ilu_colour_packed_row_ld(
   }
   if (UPPER) {
     float a[26];
-    load_packed(D, 0, nc, i, a);
-    const float d = DS[i];
+    load_packed_once(D, 0, nc, i, a, pol);
+    const float d = ld_once(DS + i, pol);
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       float x = 0.0f;
@@ -522,9 +603,14 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, SlotPtr<const T> A
   const T* __restrict__ x = sat<BATCH>(xp);
   const T* __restrict__ b = bp.p ? sat<BATCH>(bp) : nullptr;
   T* __restrict__ y = sat<BATCH>(yp);
+  constexpr bool G = std::is_same<T, float>::value;  // two-chunk gathers
   T acc[5], xi[5];
+  if constexpr (G) {
+    gather5(x, i, xi);
+  } else {
 #pragma unroll
-  for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)i * 5 + v];
+    for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)i * 5 + v];
+  }
 #pragma unroll
   for (int r = 0; r < 5; ++r) {
     T s = T(0);
@@ -536,8 +622,12 @@ __global__ void __launch_bounds__(256) spmv_kernel(DevMesh m, SlotPtr<const T> A
   for (int q = 0; q < 4; ++q) {
     const int j = m.adj[q * nc + i];
     if (j < 0) continue;
+    if constexpr (G) {
+      gather5(x, j, xi);
+    } else {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)j * 5 + v];
+      for (int v = 0; v < 5; ++v) xi[v] = x[(int64_t)j * 5 + v];
+    }
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -573,13 +663,15 @@ __global__ void __launch_bounds__(256) spmv_packed_kernel(
     const int j = m.adj[(s - 1) * nc + i];
     jn[s] = j >= 0 ? j : i;
   }
+  const uint64_t pol = l2_evict_first();
 #pragma unroll
   for (int s = 0; s < 5; ++s) {
-    const float sc = S[(int64_t)s * nc + i];
+    const float sc = ld_once(S + (int64_t)s * nc + i, pol);
     float xs[5], a[26];
+    gather5(x, jn[s], xs);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) xs[v] = sc * x[(int64_t)jn[s] * 5 + v];
-    load_packed(H, s, nc, i, a);
+    for (int v = 0; v < 5; ++v) xs[v] *= sc;
+    load_packed_once(H, s, nc, i, a, pol);
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
@@ -709,6 +801,14 @@ struct BasisIO {
 #pragma unroll
     for (int e = 0; e < W; ++e) x[e] = (A)p.v[e];
   }
+  // the same with the evict_first policy (a pass over the basis that is not read again soon)
+  template <class A>
+  __device__ static __forceinline__ void load_once(const B* V, int64_t g, A* x, uint64_t pol) {
+    const uint4 u = ld_once(reinterpret_cast<const uint4*>(V) + g, pol);
+    const Pack16<T> p = *reinterpret_cast<const Pack16<T>*>(&u);
+#pragma unroll
+    for (int e = 0; e < W; ++e) x[e] = (A)p.v[e];
+  }
   template <class A>
   __device__ static __forceinline__ void store(B* V, int64_t g, const A* x) {
     Pack16<T> p;
@@ -726,7 +826,14 @@ struct BasisIO<float, __half> {
   static constexpr int W = 8;  // 16-byte loads of eight FP16 entries
   template <class A>
   __device__ static __forceinline__ void load(const __half* V, int64_t g, A* x) {
-    const uint4 u = reinterpret_cast<const uint4*>(V)[g];
+    unpack(reinterpret_cast<const uint4*>(V)[g], x);
+  }
+  template <class A>
+  __device__ static __forceinline__ void load_once(const __half* V, int64_t g, A* x, uint64_t pol) {
+    unpack(ld_once(reinterpret_cast<const uint4*>(V) + g, pol), x);
+  }
+  template <class A>
+  __device__ static __forceinline__ void unpack(const uint4 u, A* x) {
     const unsigned w4[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -768,6 +875,8 @@ __global__ void __launch_bounds__(256) gs_dots_kernel(SlotPtr<const B> Vp, int64
   constexpr int NP = W / P::W;  // 16-byte vector packs per granule
   const B* __restrict__ V = Vp.at();
   const T* __restrict__ w = wp.at();
+  // the basis with evict_first: w stays in L2 for the update pass that reads it next
+  const uint64_t pol = l2_evict_first();
   A acc[NV + 1];
 #pragma unroll
   for (int k = 0; k <= NV; ++k) acc[k] = A(0);
@@ -786,7 +895,7 @@ __global__ void __launch_bounds__(256) gs_dots_kernel(SlotPtr<const B> Vp, int64
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       A vk[W];
-      IO::load(V + (int64_t)k * ldv, g, vk);
+      IO::load_once(V + (int64_t)k * ldv, g, vk, pol);
 #pragma unroll
       for (int e = 0; e < W; ++e) acc[k] += vk[e] * wv[e];
     }
@@ -870,6 +979,7 @@ __global__ void __launch_bounds__(256) gs_update_kernel(SlotPtr<B> outp, SlotPtr
   T* w = wp.at();
   B* out = MODE == GS_REORTH ? nullptr : outp.at();
   T* outx = kCopy && MODE != GS_REORTH ? outxp.at() : nullptr;
+  const uint64_t pol = l2_evict_first();
   A c[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) c[k] = coef[k];
@@ -890,7 +1000,9 @@ __global__ void __launch_bounds__(256) gs_update_kernel(SlotPtr<B> outp, SlotPtr
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       A vk[W];
-      IO::load(V + (int64_t)k * ldv, g, vk);
+      // evict_first except in the second pass, which reads V again in the same loop
+      if constexpr (MODE == GS_REORTH) IO::load(V + (int64_t)k * ldv, g, vk);
+      else IO::load_once(V + (int64_t)k * ldv, g, vk, pol);
 #pragma unroll
       for (int e = 0; e < W; ++e) x[e] -= c[k] * vk[e];
     }
