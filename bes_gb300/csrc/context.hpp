@@ -85,7 +85,8 @@ struct GmresDev {
   int32_t* cycles = nullptr;  // [slot] restart cycles of this solve
   double* dev = nullptr;      // [slot][kGsLd] Gram-Schmidt scalars (FP64)
   float* devf = nullptr;      // [slot][kGsLd] their FP32 copies
-  unsigned long long* counters = nullptr;  // [2] Arnoldi and restart-cycle bodies executed
+  unsigned long long* counters = nullptr;  // [3] Arnoldi, restart-cycle and second-pass bodies
+                                           // executed
 };
 
 // What one implicit step reports per slot (read back once per step).
@@ -175,9 +176,9 @@ struct ImplicitBuffers {
   // sections (top level, one slot's assembly, one Arnoldi step, one restart-cycle end)
   cudaGraphExec_t step_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   int64_t nodes_top[2] = {0, 0}, nodes_slot[2] = {0, 0}, nodes_arn[2] = {0, 0},
-          nodes_loop[2] = {0, 0};
-  cudaStream_t cap[2] = {nullptr, nullptr};  // streams capturing conditional bodies
-  unsigned long long counters_host[2] = {0, 0};
+          nodes_loop[2] = {0, 0}, nodes_gs2[2] = {0, 0};
+  cudaStream_t cap[3] = {nullptr, nullptr, nullptr};  // streams capturing conditional bodies
+  unsigned long long counters_host[3] = {0, 0, 0};
   std::vector<SlotCtl> ctl;    // [slot]
   int64_t step_count = 0;      // step calls of the context
   int64_t total_lin_iters = 0;

@@ -360,8 +360,8 @@ void enqueue_spmv(const Sys<T, B>& S, cudaStream_t s, SlotPtr<const T> x, SlotPt
 // Body of the IF node of Arnoldi step j (slots with a running cycle): w = A M^{-1} v_j,
 // Gram-Schmidt against v_0..v_j, v_{j+1}, and the Givens update of the Hessenberg column.
 template <class T, class B>
-void enqueue_arnoldi(const Sys<T, B>& S, cudaStream_t s, int j, const GmresParam& P,
-                     const GmresHandles& h) {
+int enqueue_arnoldi(const Sys<T, B>& S, cudaStream_t s, int j, const GmresParam& P,
+                    const GmresHandles& h, int64_t* gs2_kernels) {
   bes_ctx* c = S.c;
   // with one slot the IF node alone decides whether the step runs: no per-block flag load
   const int32_t* cyc = S.nslot > 1 ? c->imp.gm.cyc : nullptr;
@@ -377,18 +377,31 @@ void enqueue_arnoldi(const Sys<T, B>& S, cudaStream_t s, int j, const GmresParam
   launch_gs_dots<T, B>(nv, S.vgrid, s, Vb, S.ldv, S.cvec(S.W), S.N, S.red(), cyc);
   reduce_slots_kernel<<<dim3(nv + 1, S.nslot), 256, 0, s>>>(S.cred(), kRedBlocks, nv + 1, 0,
                                                             S.dev(), cyc);
-  gs_decide_kernel<<<dim3(1, S.nslot), 64, 0, s>>>(S.dev(), S.devf(), nv, 1, cyc);
+  gs_decide_kernel<<<dim3(1, S.nslot), 64, 0, s>>>(S.dev(), S.devf(), nv, 1, cyc, h.gs2[j],
+                                                    h.on, nullptr);
   launch_gs_update<T, B, GS_FINAL1>(nv, S.vgrid, s, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
                                     S.ldv, S.cdev(), S.cdevf(), S.N, S.red(), cyc);
-  launch_gs_update<T, B, GS_REORTH>(nv, S.vgrid, s, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
+  // the second pass (rare): in the step graph an IF node that runs only when a slot needs it,
+  // so that its four launches cost nothing otherwise
+  cudaStream_t s2 = s;
+  if (h.on) {
+    s2 = c->imp.cap[2];
+    if (const int rc = begin_conditional(c, s, s2, h.gs2[j], cudaGraphCondTypeIf)) return rc;
+  }
+  launch_gs_update<T, B, GS_REORTH>(nv, S.vgrid, s2, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
                                     S.ldv, S.cdev(), S.cdevf(), S.N, S.red(), cyc);
-  reduce_slots_kernel<<<dim3(nv + 1, S.nslot), 256, 0, s>>>(S.cred(), kRedBlocks, nv + 1, 0,
-                                                            S.dev(kGsH2), cyc);
-  gs_decide_kernel<<<dim3(1, S.nslot), 64, 0, s>>>(S.dev(), S.devf(), nv, 2, cyc);
-  launch_gs_update<T, B, GS_FINAL2>(nv, S.vgrid, s, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
+  reduce_slots_kernel<<<dim3(nv + 1, S.nslot), 256, 0, s2>>>(S.cred(), kRedBlocks, nv + 1, 0,
+                                                             S.dev(kGsH2), cyc);
+  gs_decide_kernel<<<dim3(1, S.nslot), 64, 0, s2>>>(S.dev(), S.devf(), nv, 2, cyc, h.gs2[j],
+                                                     h.on, h.on ? c->imp.gm.counters + 2 : nullptr);
+  launch_gs_update<T, B, GS_FINAL2>(nv, S.vgrid, s2, S.basis(j + 1), S.vec(S.Vx), S.vec(S.W), Vb,
                                     S.ldv, S.cdev(), S.cdevf(), S.N, S.red(), cyc);
+  if (h.on) {
+    if (const int rc = end_conditional(c, s2, gs2_kernels)) return rc;
+  }
   gmres_givens_kernel<<<1, S.nthr, 0, s>>>(c->imp.gm, P, h, S.nslot, j);
   stamp(c, s, PROF_ORTHO, 0);
+  return BES_OK;
 }
 
 // End of a restart cycle (slots whose solve runs): x += M^{-1} V y, r = b - A x, and the
@@ -655,7 +668,7 @@ double* result_norms(StepResult* res, int k) {
 
 // End every capture still open after a failure, so the streams are usable again.
 void abandon_capture(bes_ctx* c) {
-  cudaStream_t ss[3] = {c->imp.cap[1], c->imp.cap[0], c->stream};
+  cudaStream_t ss[4] = {c->imp.cap[2], c->imp.cap[1], c->imp.cap[0], c->stream};
   for (cudaStream_t s : ss) {
     cudaStreamCaptureStatus st;
     if (s && cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
@@ -685,8 +698,10 @@ int capture_step(bes_ctx* c, int prof, cudaGraph_t* out) {
   std::memset(&gh, 0, sizeof(gh));
   gh.on = 1;
   IMP_TRY(c, cudaGraphConditionalHandleCreate(&gh.loop, g, 0, cudaGraphCondAssignDefault));
-  for (int j = 0; j < o.gmres_restart; ++j)
+  for (int j = 0; j < o.gmres_restart; ++j) {
     IMP_TRY(c, cudaGraphConditionalHandleCreate(&gh.arn[j], g, 0, cudaGraphCondAssignDefault));
+    IMP_TRY(c, cudaGraphConditionalHandleCreate(&gh.gs2[j], g, 0, cudaGraphCondAssignDefault));
+  }
   const GmresParam P{o.gmres_restart, o.linear_solver_max_iter, o.linear_solver_tol};
   int rc;
   enqueue_residual_all(c, s0, hs, 1);
@@ -700,7 +715,7 @@ int capture_step(bes_ctx* c, int prof, cudaGraph_t* out) {
   if ((rc = begin_conditional(c, s0, s1, gh.loop, cudaGraphCondTypeWhile))) return rc;
   for (int j = 0; j < o.gmres_restart; ++j) {
     if ((rc = begin_conditional(c, s1, s2, gh.arn[j], cudaGraphCondTypeIf))) return rc;
-    enqueue_arnoldi(S, s2, j, P, gh);
+    if ((rc = enqueue_arnoldi(S, s2, j, P, gh, &I.nodes_gs2[prof]))) return rc;
     if ((rc = end_conditional(c, s2, &I.nodes_arn[prof]))) return rc;
   }
   enqueue_cycle_end(S, s1, P, gh);
@@ -722,6 +737,7 @@ int build_step_graph(bes_ctx* c, int prof) {
   if (!I.cap[0]) {
     IMP_TRY(c, cudaStreamCreateWithFlags(&I.cap[0], cudaStreamNonBlocking));
     IMP_TRY(c, cudaStreamCreateWithFlags(&I.cap[1], cudaStreamNonBlocking));
+    IMP_TRY(c, cudaStreamCreateWithFlags(&I.cap[2], cudaStreamNonBlocking));
   }
   if (!I.tuned) {
     const int rc = tune_sweep<T, B>(c);
@@ -819,7 +835,7 @@ int run_steps(bes_ctx* c, int64_t n, double* history) {
     if (rc) return rc;
     IMP_TRY(c, cudaGraphLaunch(I.step_graph[prof][c->cur], c->stream));
     int nan = 0, sync_err = 0;
-    unsigned long long cnt[2];
+    unsigned long long cnt[3];
     IMP_TRY(c, cudaMemcpyAsync(I.res_host.data(), I.res, ns * sizeof(StepResult),
                                cudaMemcpyDeviceToHost, c->stream));
     IMP_TRY(c, cudaMemcpyAsync(cnt, I.gm.counters, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
@@ -840,9 +856,9 @@ int run_steps(bes_ctx* c, int64_t n, double* history) {
     for (int k = 0; k < ns; ++k) nact += act[k];
     c->launches += I.nodes_top[prof] + nact * I.nodes_slot[prof] +
                    (int64_t)(cnt[0] - I.counters_host[0]) * I.nodes_arn[prof] +
-                   (int64_t)(cnt[1] - I.counters_host[1]) * I.nodes_loop[prof];
-    I.counters_host[0] = cnt[0];
-    I.counters_host[1] = cnt[1];
+                   (int64_t)(cnt[1] - I.counters_host[1]) * I.nodes_loop[prof] +
+                   (int64_t)(cnt[2] - I.counters_host[2]) * I.nodes_gs2[prof];
+    for (int q = 0; q < 3; ++q) I.counters_host[q] = cnt[q];
     if ((rc = check_step_nan(c, nan))) return rc;
     int status = BES_OK;
     for (int k = 0; k < ns; ++k) {
@@ -1043,7 +1059,7 @@ int implicit_allocate(bes_ctx* c) {
   for (int32_t** p : ints) rc |= imp_malloc(c, (void**)p, ns * sizeof(int32_t));
   rc |= imp_malloc(c, (void**)&g.dev, ns * kGsLd * sizeof(double));
   rc |= imp_malloc(c, (void**)&g.devf, ns * kGsLd * sizeof(float));
-  rc |= imp_malloc(c, (void**)&g.counters, 2 * sizeof(unsigned long long));
+  rc |= imp_malloc(c, (void**)&g.counters, 3 * sizeof(unsigned long long));
   rc |= imp_malloc(c, (void**)&I.res, ns * sizeof(StepResult));
   rc |= imp_malloc(c, (void**)&I.cfl_dev, ns * sizeof(double));
   rc |= imp_malloc(c, (void**)&I.act, ns * sizeof(int32_t));
@@ -1060,7 +1076,7 @@ int implicit_allocate(bes_ctx* c) {
   IMP_TRY(c, cudaMemset(I.A, 0, 125 * nc * I.tsize * msl));  // empty slots stay zero
   IMP_TRY(c, cudaMemset(g.lin, 0, ns * sizeof(int32_t)));
   IMP_TRY(c, cudaMemset(g.cyc, 0, ns * sizeof(int32_t)));
-  IMP_TRY(c, cudaMemset(g.counters, 0, 2 * sizeof(unsigned long long)));
+  IMP_TRY(c, cudaMemset(g.counters, 0, 3 * sizeof(unsigned long long)));
   IMP_TRY(c, cudaMemset(I.guard_dev, 0, sizeof(int32_t)));
   IMP_TRY(c, cudaMemset(I.sync_count, 0, sizeof(unsigned)));
   IMP_TRY(c, cudaMemset(I.sync_gen, 0, sizeof(unsigned)));

@@ -912,9 +912,18 @@ __global__ void __launch_bounds__(256) gs_dots_kernel(SlotPtr<const B> Vp, int64
 
 // Decide after a reduction (grid (1, slots)): stage 1 (after pass 1) sets the second-pass
 // flag and, without a second pass, 1/h_{j+1,j}; stage 2 (after pass 2) sets 1/h_{j+1,j} from
-// the second pass.
+// the second pass.  Inside the step graph the second pass is the body of an IF node on
+// `second` (set_second != 0): stage 1 sets it to 1 for a slot that needs the pass, and stage 2,
+// which runs inside that body, sets it back to 0 for the next Arnoldi step of this index and
+// counts the body's executions in *passes.
 static __global__ void gs_decide_kernel(SlotPtr<double> devp, SlotPtr<float> devfp, int nv,
-                                        int stage, const int32_t* run) {
+                                        int stage, const int32_t* run,
+                                        cudaGraphConditionalHandle second, int set_second,
+                                        unsigned long long* passes) {
+  if (stage == 2 && blockIdx.y == 0 && threadIdx.x == 0) {
+    if (set_second) cudaGraphSetConditional(second, 0u);
+    if (passes) ++*passes;
+  }
   if (slot_idle(run)) return;
   double* __restrict__ dev = devp.at();
   float* __restrict__ devf = devfp.at();
@@ -931,6 +940,7 @@ static __global__ void gs_decide_kernel(SlotPtr<double> devp, SlotPtr<float> dev
     const double est = nw2 - s;
     const bool reorth = !(est > kReorthTheta2 * nw2);
     dev[kGsFlag] = reorth ? 1.0 : 0.0;
+    if (reorth && set_second) cudaGraphSetConditional(second, 1u);
     const double hn = reorth ? 0.0 : sqrt(est);
     dev[kGsNorm] = hn;
     dev[kGsInv] = hn > 0.0 ? 1.0 / hn : 0.0;
@@ -1232,6 +1242,7 @@ struct GmresParam {
 struct GmresHandles {
   cudaGraphConditionalHandle loop;              // WHILE over restart cycles
   cudaGraphConditionalHandle arn[kMaxRestart];  // IF of Arnoldi step j
+  cudaGraphConditionalHandle gs2[kMaxRestart];  // IF of step j's second Gram-Schmidt pass
   int on;                                       // 0: not inside a conditional graph
 };
 

@@ -198,3 +198,58 @@ def test_profile_counts_follow_the_iterations():
     assert p["gram_schmidt"][1] == its + 2 * cycles + 6
     assert all(v[0] > 0 for k, v in p.items() if v[1])
     assert a.profile(False)["spmv"] == (0.0, 0)
+
+
+@pytest.mark.gpu
+def test_second_gram_schmidt_pass_behind_its_if_node():
+    """The second Gram-Schmidt pass is an IF node of the step graph that the first pass's
+    decision opens.  On a 6-cell mesh (30 unknowns) GMRES converges by orders of magnitude per
+    iteration, so the first pass cancels most of w and the second pass runs (counted); the
+    FP64 system still reaches the oracle's states, which run the same conditional pass.  A
+    batch whose slots need the pass at different Arnoldi steps gives each slot's
+    single-context run bit for bit (16-bit storage).  Solved to 1e-10 on the
+    6,912-cell channel the iterates equal the oracle's with the same linear-iteration counts."""
+    from bes_gb300 import lib
+
+    kw = dict(solver_type=1, local_time_step=1, courant_num=10.0, freestream_mach=(0.84, 0, 0),
+              linear_solver=1, linear_solver_tol=1e-13, linear_solver_max_iter=300,
+              gmres_restart=30, cfl_ramp_steps=8, cfl_ramp_start=10.0, cfl_ramp_end=500.0)
+    okw = dict(solver=1, local_dt=1, cfl=10.0, mach=(0.84, 0, 0), lin_precond=1, lin_maxiter=300,
+               lin_restart=30, ramp_steps=8, ramp_cfl0=10.0, ramp_cfl1=500.0)
+    tiny = meshgen.bump_channel(1, 1, 1, 0.08)
+    ctx = context(tiny, **kw)
+    h = ctx.implicit_steps(3)
+    passes = ctx.counters()["gram_schmidt_second_passes"]
+    O = pyoracle.Oracle(tiny, lin_tol=1e-13, **okw)
+    O.set_ilu_order(ctx.ilu_order())
+    ho = O.implicit_run(3)
+    assert passes > 0
+    assert np.all(np.abs(h[:, 12] - ho[:, 12]) <= 1)
+    assert rel_err(ctx.get_state(), O.get_state()) <= 1e-10
+    ctx.close()
+
+    machs = [(0.84, 0.0, 0.0), (0.7, 0.05, 0.0), meshgen.freestream_mach_vector(0.6, 3.0, -2.0)]
+    kp = dict(kw, precision=2, linear_solver_tol=1e-5)
+    kp.pop("freestream_mach")
+    bat = lib.Context(tiny, lib.default_options(**kp), machs=machs)
+    hb = bat.implicit_steps(3)
+    Ub = bat.get_state()
+    assert bat.counters()["gram_schmidt_second_passes"] > 0
+    bat.close()
+    for q, m in enumerate(machs):
+        one = context(tiny, freestream_mach=m, **kp)
+        h1 = one.implicit_steps(3)
+        assert np.array_equal(h1, hb[:, q])
+        assert np.array_equal(one.get_state(), Ub[q])
+        one.close()
+
+    mesh = meshgen.bump_channel(24, 8, 6, 0.08)
+    ctx = context(mesh, **dict(kw, linear_solver_tol=1e-10))
+    h = ctx.implicit_steps(3)
+    O = pyoracle.Oracle(mesh, lin_tol=1e-10, **okw)
+    O.set_ilu_order(ctx.ilu_order())
+    ho = O.implicit_run(3)
+    assert np.array_equal(h[:, 12], ho[:, 12])
+    assert hist_rel_err(h[:, :12], ho[:, :12]) <= 1e-9
+    assert rel_err(ctx.get_state(), O.get_state()) <= 1e-9
+    ctx.close()
