@@ -134,9 +134,10 @@ WORKLOADS = {
                                            linear_solver_max_iter=300, gmres_restart=30,
                                            cfl_ramp_steps=50, cfl_ramp_start=10.0,
                                            cfl_ramp_end=1000.0, precision=2)),
-    # production form at scale: the Gaussian-bump box at 200x100x200 hexes (24.0M tets), 16
-    # conditions (seed 3) in one batched implicit context (precision 2, the benchmark's
-    # GMRES settings); a throughput measurement of whole batched steps, not converged solves
+    # production form at scale: the Gaussian-bump box at 200x100x200 hexes (24.0M tets), the
+    # 16 conditions of seed 3, as many of them as one GB300's memory holds as slots of one
+    # batched implicit context (precision 2, the benchmark's GMRES settings); a throughput
+    # measurement of whole batched steps, not converged solves
     "implicit_gauss_24m_16": dict(kind="scale", mesh=("gauss", 200, 100, 200, 1.05), conds=(3, 16),
                                   opts=dict(solver_type=1, local_time_step=1, courant_num=10.0,
                                             linear_solver=1, linear_solver_tol=1e-2,
@@ -982,16 +983,29 @@ def run_isweep(args, wl, torch, mesh, clocks):
             "per_condition_sampled": rows, "clocks": clk}
 
 
+# Device bytes per cell of a batched implicit context with the 16-bit storage (precision 2):
+# per slot (state, face-side states, fluxes, time steps, the 16-bit matrix, factors and
+# inverse diagonal, the FP16 basis of 31 vectors, the FP32 and FP64 Krylov vectors: about
+# 1.26 kB, rounded up) and shared by the slots (mesh and geometry, the FP32 assembly and
+# factorisation scratch: about 1.9 kB, rounded up)
+SLOT_BYTES_PER_CELL = 1350
+SHARED_BYTES_PER_CELL = 2200
+
+
 def run_scale(args, wl, torch, mesh, clocks):
-    """Batched implicit steps of many conditions on a large mesh: one step = one implicit step
-    of every condition (stepped one after another through the shared implicit buffers); value =
-    conditions x cells x steps / event-timed device time.  Reports the device memory the
-    context holds and its set-up time (host mesh build, renumbering, upload)."""
+    """Batched implicit steps of many conditions on a large mesh: one step = one graph launch
+    advancing every slot of the context; value = slots x cells x steps / event-timed device
+    time.  The slots are the first of the workload's conditions, as many as the device memory
+    holds.  Reports the device memory the context holds and its set-up time (host mesh build,
+    renumbering, upload)."""
     from bes_gb300 import lib, meshgen
-    seed, n = wl["conds"]
-    machs = np.array([meshgen.freestream_mach_vector(*c)
-                      for c in meshgen.sample_conditions(n, seed)])
+    seed, n_drawn = wl["conds"]
     free0, total = torch.cuda.mem_get_info()
+    nc_mesh = int(mesh.n_cells)
+    fit = int((free0 - 8e9 - SHARED_BYTES_PER_CELL * nc_mesh) // (SLOT_BYTES_PER_CELL * nc_mesh))
+    n = max(1, min(n_drawn, fit))
+    machs = np.array([meshgen.freestream_mach_vector(*c)
+                      for c in meshgen.sample_conditions(n_drawn, seed)])[:n]
     t0 = time.perf_counter()
     ctx = lib.Context(mesh, lib.default_options(**wl["opts"]), machs=machs)
     t_setup = time.perf_counter() - t0
@@ -1023,7 +1037,7 @@ def run_scale(args, wl, torch, mesh, clocks):
             "dtype": "f32 system stored as fp16 blocks, fp16 Krylov basis / f64 residual and "
                      "update", "data": "synthetic",
             "config": {"workload": args.workload, "cells": nc, "conditions": n,
-                       "parallelism": "replicas1",
+                       "conditions_drawn": n_drawn, "parallelism": "replicas1",
                        "l2": "inputs larger than L2 (a step streams tens of GB)",
                        "linear_iterations_per_condition_step": float(hist[:, :, 12].mean()),
                        "device_memory_gb": (free0 - free1) / 1e9,
