@@ -225,9 +225,17 @@ def test_besi_precision_key(word, value):
     assert o.precision == value
 
 
+@pytest.mark.parametrize("word,value", [("AUTO", 0), ("PER_COLOUR", 1), ("PERSISTENT", 2),
+                                        ("PER_COLOUR_LOADS_FIRST", 3)])
+def test_besi_sweep_kernel_key(word, value):
+    with tempfile.TemporaryDirectory() as d:
+        o, _ = lib.options_from_besi(_write(d, f"SWEEP_KERNEL = {word}\n"))
+    assert o.sweep_kernel == value
+
+
 @pytest.mark.parametrize("line", ["NOT_A_KEY = 1", "SOLVER_TYPE = SEMI", "FLUX_SCHEME = AUSM",
                                   "FREESTREAM_MACH = 0.5, 0", "GMRES_RESTART = 33",
-                                  "PRECISION = FP16"])
+                                  "PRECISION = FP16", "SWEEP_KERNEL = EARLY"])
 def test_besi_parser_is_strict(line):
     with tempfile.TemporaryDirectory() as d:
         p = _write(d, "MESH_FORMAT = GMSH\n" + line + "\n")
