@@ -52,6 +52,8 @@ __device__ __forceinline__ bool slot_idle(const int32_t* run) {
 // vectors whose values the neighbour gathers read again, and every gathered neighbour costs a
 // DRAM sector: the 2.16M-cell SpMV read 829 MB from DRAM against 696 MB of compulsory traffic.
 // Loaded with an evict_first policy the matrix words leave the vectors in L2 (696 MB).
+// ld_once is a read-only (non-coherent) load that the compiler may move: only for words that
+// no thread writes while the kernel runs.
 __device__ __forceinline__ uint64_t l2_evict_first() {
   uint64_t p;
   asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
