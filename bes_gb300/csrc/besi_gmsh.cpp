@@ -211,7 +211,7 @@ extern "C" int bes_options_from_besi(const char* path, bes_options* o, char* mes
       if (w < 0)
         return bad("SWEEP_KERNEL must be AUTO, PER_COLOUR, PERSISTENT or PER_COLOUR_LOADS_FIRST");
       o->sweep_kernel = w;
-    } else if (key == "JACOBIAN_REPEAT") {  // additive: 5 reproduces the reference
+    } else if (key == "JACOBIAN_REPEAT") {  // additive: without it, the reference's count
       if (!num(0, x) || x < 1) return bad("JACOBIAN_REPEAT must be >= 1");
       o->jacobian_repeat = (int32_t)x;
     } else {

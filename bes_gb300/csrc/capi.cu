@@ -163,7 +163,7 @@ void bes_options_default(bes_options* o) {
   o->linear_solver_max_iter = 1000;
   o->gmres_restart = 30;
   o->linear_solver_tol = 1e-7;
-  o->jacobian_repeat = 5;
+  o->jacobian_repeat = 0;  // the reference's: once per conserved variable of the mesh
   o->precision = 0;
   o->cfl_ramp_steps = 0;
 }
@@ -204,6 +204,10 @@ int create_context(const bes_mesh_arrays* mesh, const bes_options* opt, int n_co
                       ctx->ref, err)) {
     return BES_ERR_MESH;
   }
+  // Q9: the reference adds every Jacobian block once per conserved variable (its addToBlock
+  // sits inside the loop over the variables, src/SolverImplicit.cpp:425-455, 465-502): five
+  // times in 3-D, four times in 2-D
+  if (ctx->opt.jacobian_repeat <= 0) ctx->opt.jacobian_repeat = ctx->ref.dim == 2 ? 4 : 5;
   build_soa(ctx->ref, opt->venkatakrishnan_factor, opt->muscl_face_vector != 0, true, ctx->soa);
   ctx->nodes.assign(mesh->nodes, mesh->nodes + mesh->n_nodes * 3);
   ctx->tets.assign(mesh->tets, mesh->tets + mesh->n_tets * (bes_mesh_dim(mesh) + 1));

@@ -77,7 +77,9 @@ typedef struct {
   int32_t linear_solver_max_iter; /* LINEAR_SOLVER_MAX_ITER (default 1000) */
   int32_t gmres_restart;          /* GMRES_RESTART (additive, default 30) */
   double linear_solver_tol;       /* LINEAR_SOLVER_ABS_TOL: relative to |b| (default 1e-7) */
-  int32_t jacobian_repeat;        /* times each Jacobian block is added (Q9, default 5) */
+  int32_t jacobian_repeat;        /* times each Jacobian block is added (Q9); 0, the default:
+                                     once per conserved variable of the mesh, 5 in 3-D and 4
+                                     in 2-D, as the reference (src/SolverImplicit.cpp:425-502) */
   int32_t precision;              /* PRECISION (additive): 0 FP64, 1 FP32 linear solve,
                                      2 FP32 linear solve with the matrix and factors stored
                                      as FP16 blocks with a power-of-two scale per block and

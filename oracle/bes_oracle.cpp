@@ -720,7 +720,8 @@ static void implicit_step(Oracle& O, double* hist) {
     jac_kind(O, M.kind[f], &M.nhat[f * 3], U1L, U1R, &O.JL[f * 25], &O.JR[f * 25]);
   }
   // Assembly, per cell in increasing face id: identical to the face loop's sequence of
-  // atomic adds at one thread.  Every block is added jacobian_repeat (= 5, Q9) times.
+  // atomic adds at one thread.  Every block is added jacobian_repeat times (Q9: once per
+  // conserved variable, 5 in 3-D and 4 in 2-D).
   const int rep = O.o.jacobian_repeat;
 #pragma omp parallel for num_threads(O.threads)
   for (int64_t c = 0; c < M.nc; ++c) {
@@ -835,7 +836,8 @@ void* bor_create(const double* nodes, int64_t nv, const int64_t* tets, int64_t n
   o.local_dt = op->local_dt;
   o.n_stage = op->n_stage;
   o.muscl_exact = op->muscl_exact;
-  o.jacobian_repeat = op->jacobian_repeat;
+  // 0: the reference's count, once per conserved variable (src/SolverImplicit.cpp:425-502)
+  o.jacobian_repeat = op->jacobian_repeat > 0 ? op->jacobian_repeat : (dim == 2 ? 4 : 5);
   o.lin_precond = op->lin_precond;
   o.lin_restart = op->lin_restart;
   o.lin_maxiter = op->lin_maxiter;

@@ -50,7 +50,7 @@ class _Opts(ctypes.Structure):
     ]
 
 
-DEFAULTS = dict(solver=0, local_dt=1, n_stage=4, muscl_exact=0, jacobian_repeat=5,
+DEFAULTS = dict(solver=0, local_dt=1, n_stage=4, muscl_exact=0, jacobian_repeat=0,
                 lin_precond=0, lin_restart=30, lin_maxiter=1000, ramp_steps=0, threads=1,
                 cfl=0.8, cfl_max=0.0, cfl_exp=(1.0, 1.0),
                 alpha=(0.0833, 0.2069, 0.4265, 1.0), venkat_k=5.0, harten=0.05,

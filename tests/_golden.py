@@ -22,6 +22,9 @@ CASES = ["explicit_bump_local", "explicit_bump_global", "explicit_gauss_pitch",
 # triangle meshes (the reference's 2-D path); the fixtures pad per-cell data to the 3-D
 # layout: five conserved variables (rho w = 0) and four face slots (the fourth -1)
 CASES_2D = ["explicit_bump2d_local"]
+# the reference's 2-D implicit run (its 4x4-block systems solved through the linear-solver
+# facade as 5x5 blocks with a decoupled spanwise-momentum row)
+CASES_2D_IMPLICIT = ["implicit_bump2d_ilu0"]
 
 
 def load(name):

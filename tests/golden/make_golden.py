@@ -54,10 +54,16 @@ CASES = {
                                   lin_maxiter=300),
                              12, "implicit", True),
     # 2-D (triangles, 4 conserved variables; fixtures in the 3-D layout, see the harness).
-    # Implicit 2-D is not pinned: the reference build's linear-solver facade is 5x5-block.
+    # The implicit case's 4x4-block systems go through the linear-solver facade as 5x5 blocks
+    # with a decoupled spanwise-momentum row (oracle/ref/stubs/amgcl/facade.hpp).
     "explicit_bump2d_local": (lambda: meshgen.bump_channel_2d(24, 8, 0.08),
                               dict(solver="EXPLICIT", local="YES", cfl=0.8, mach=(0.6, 0.04, 0)),
                               50, "explicit", "geometry"),
+    "implicit_bump2d_ilu0": (lambda: meshgen.bump_channel_2d(24, 8, 0.08),
+                             dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
+                                  mach=(0.6, 0.04, 0), smoother="ILU0", lin_tol=1e-2,
+                                  lin_maxiter=300),
+                             12, "implicit", False),
     "implicit_bump_ilu0": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
                            dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
                                 mach=(0.84, 0, 0), smoother="ILU0", lin_tol=1e-2,

@@ -2,12 +2,12 @@
 
 The explicit path is pinned to the reference's own 2-D run in test_gpu_explicit.py (residual
 history and final state within 1e-10) and here against the oracle with a global time step.
-The reference build cannot run its implicit solver on a 2-D mesh (its linear-solver facade is
-sized for five conserved variables), so the implicit path on triangles is checked against the
-oracle's restatement (the same five-variable formulation with zero spanwise momentum, given
-the GPU's block-ILU(0) order) and through properties: it converges to the steady state of the
-explicit path (the same discrete residual R(U) = 0), the FP32 system tracks the FP64 one, and
-the spanwise momentum stays zero.
+The implicit path on triangles is checked against the oracle's restatement (the same
+five-variable formulation with zero spanwise momentum, given the GPU's block-ILU(0) order),
+which the reference's own 2-D implicit run pins (tests/test_oracle_golden.py; each Jacobian
+block added four times in 2-D, the default), and through properties: it converges to the
+steady state of the explicit path (the same discrete residual R(U) = 0), the FP32 system
+tracks the FP64 one, and the spanwise momentum stays zero.
 
 Tolerances: explicit 1e-10 (as the 3-D path); implicit steps against the oracle 1e-9 with equal
 linear-iteration counts (as the 3-D path); steady states of the two solvers 1e-7 relative to
