@@ -25,6 +25,8 @@ CASES_2D = ["explicit_bump2d_local"]
 # the reference's 2-D implicit run (its 4x4-block systems solved through the linear-solver
 # facade as 5x5 blocks with a decoupled spanwise-momentum row)
 CASES_2D_IMPLICIT = ["implicit_bump2d_ilu0"]
+# implicit histories only (no operator dumps): the oracle against the reference's own steps
+CASES_IMPLICIT_HISTORY = ["implicit_bump_global", "implicit_gauss_pitch"]
 
 
 def load(name):

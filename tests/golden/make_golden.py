@@ -69,6 +69,17 @@ CASES = {
                                 mach=(0.84, 0, 0), smoother="ILU0", lin_tol=1e-2,
                                 lin_maxiter=300),
                            12, "implicit", True),
+    # implicit with a global time step, and on the pitched Gaussian box (histories only)
+    "implicit_bump_global": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+                             dict(solver="IMPLICIT", local="NO", cfl=10.0, cfl_max=1000.0,
+                                  mach=(0.84, 0, 0), smoother="DAMPED_JACOBI", lin_tol=1e-2,
+                                  lin_maxiter=300),
+                             8, "implicit", False),
+    "implicit_gauss_pitch": (lambda: meshgen.gaussian_box(8, 4, 8),
+                             dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
+                                  mach=meshgen.freestream_mach_vector(0.7, 3.0, -2.0),
+                                  smoother="ILU0", lin_tol=1e-2, lin_maxiter=300),
+                             8, "implicit", False),
 }
 
 # the reference's own output files (Solver::writeToFile_ after the last step, and the residual

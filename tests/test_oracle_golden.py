@@ -92,6 +92,18 @@ def test_implicit_history_matches_reference(case):
     assert rel_err(O.get_state(), ref["final_state"]) <= 1e-10
 
 
+@pytest.mark.parametrize("case", G.CASES_IMPLICIT_HISTORY)
+def test_implicit_history_matches_reference_global_dt_and_pitch(case):
+    """Implicit steps with a global time step, and on the pitched Gaussian box (block ILU(0)
+    in the reference's cell order), against the reference's own runs."""
+    ref, info = G.load(case)
+    O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
+    hist = O.implicit_run(info["steps"])
+    refh = ref["implicit_history"].reshape(-1, 12)
+    assert np.max(np.abs(hist[:, :12] - refh) / np.maximum(np.abs(refh), 1e-300)) <= 1e-10
+    assert rel_err(O.get_state(), ref["final_state"]) <= 1e-10
+
+
 @pytest.mark.parametrize("case", G.CASES_2D_IMPLICIT)
 def test_2d_implicit_history_matches_reference(case):
     """The reference's own 2-D implicit steps (triangles, 4x4 blocks) against the oracle's
