@@ -27,6 +27,9 @@ CASES_2D = ["explicit_bump2d_local"]
 CASES_2D_IMPLICIT = ["implicit_bump2d_ilu0"]
 # implicit histories only (no operator dumps): the oracle against the reference's own steps
 CASES_IMPLICIT_HISTORY = ["implicit_bump_global", "implicit_gauss_pitch"]
+# the rest of the option surface (stage coefficients, limiter and Harten constants, gas
+# constants, adaptive-CFL exponents), histories only
+CASES_OPTIONS = ["explicit_bump_options", "implicit_bump_options"]
 
 
 def load(name):
@@ -46,7 +49,8 @@ def oracle_kwargs(info):
               local_dt=1 if m["local"] == "YES" else 0, cfl=m["cfl"], mach=tuple(m["mach"]),
               fs_ramp=m.get("fs_ramp", 0), fs_frac=m.get("fs_frac", 0.5))
     if m["solver"] == "IMPLICIT":
-        kw.update(cfl_max=m["cfl_max"], cfl_exp=(1.0, 1.0),
+        kw.update(cfl_max=m["cfl_max"], cfl_exp=tuple(m.get("cfl_exp", (1.0, 1.0))),
                   lin_precond=1 if m["smoother"] == "ILU0" else 0, lin_tol=m["lin_tol"],
                   lin_maxiter=m["lin_maxiter"], lin_restart=30)
+    kw.update(m.get("oracle", {}))  # the option-surface cases' other keys
     return kw

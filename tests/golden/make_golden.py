@@ -80,6 +80,25 @@ CASES = {
                                   mach=meshgen.freestream_mach_vector(0.7, 3.0, -2.0),
                                   smoother="ILU0", lin_tol=1e-2, lin_maxiter=300),
                              8, "implicit", False),
+    # the rest of the option surface on the path: `besi` lines added to the case file, `oracle`
+    # the matching keyword arguments of the CPU restatement
+    "explicit_bump_options": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+                              dict(solver="EXPLICIT", local="YES", cfl=0.8, mach=(0.7, 0.05, 0),
+                                   besi=["MULTI_TIME_STEP_OPTIONS = 3, 0.1, 0.5, 1.0",
+                                         "VENKATAKRISHNAN_FACTOR = 2.0",
+                                         "HARTEN_CORRECTION_LIMIT = 0.2",
+                                         "SPECIFIC_HEAT_RATIO = 1.3", "GAS_CONSTANT = 300.0"],
+                                   oracle=dict(alpha=(0.1, 0.5, 1.0), venkat_k=2.0, harten=0.2,
+                                               gamma=1.3, gas_constant=300.0)),
+                              20, "explicit", False),
+    "implicit_bump_options": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+                              dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
+                                   mach=(0.7, 0.05, 0), smoother="ILU0", lin_tol=1e-2,
+                                   lin_maxiter=300, cfl_exp=(0.5, 2.0),
+                                   besi=["SPECIFIC_HEAT_RATIO = 1.3",
+                                         "VENKATAKRISHNAN_FACTOR = 2.0"],
+                                   oracle=dict(gamma=1.3, venkat_k=2.0)),
+                              8, "implicit", False),
 }
 
 # the reference's own output files (Solver::writeToFile_ after the last step, and the residual
@@ -130,15 +149,17 @@ def besi_text(mesh_path: str, out_dir: str, o: dict, steps: int) -> str:
         lines += [f"FREESTREAM_RAMP = {o['fs_ramp']}",
                   f"FREESTREAM_RAMP_START_FRAC = {o['fs_frac']!r}"]
     if o["solver"] == "IMPLICIT":
+        e0, e1 = o.get("cfl_exp", (1.0, 1.0))
         lines += [
             f"ADAPTIVE_COURANT_NUM_MAX = {o['cfl_max']!r}",
-            "ADAPTIVE_COURANT_NUM_EXPONENT = 1.0, 1.0",
+            f"ADAPTIVE_COURANT_NUM_EXPONENT = {e0!r}, {e1!r}",
             "LINEAR_SOLVER = GMRES",
             "AMG_PRECOND_COARSENER = AGGREGATION",
             f"AMG_PRECOND_SMOOTHER = {o['smoother']}",
             f"LINEAR_SOLVER_MAX_ITER = {o['lin_maxiter']}",
             f"LINEAR_SOLVER_ABS_TOL = {o['lin_tol']!r}",
         ]
+    lines += o.get("besi", [])
     return "\n".join(lines) + "\n"
 
 

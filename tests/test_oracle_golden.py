@@ -104,6 +104,25 @@ def test_implicit_history_matches_reference_global_dt_and_pitch(case):
     assert rel_err(O.get_state(), ref["final_state"]) <= 1e-10
 
 
+@pytest.mark.parametrize("case", G.CASES_OPTIONS)
+def test_option_surface_matches_reference(case):
+    """Three stage coefficients, Venkatakrishnan factor 2, Harten limit 0.2, gamma 1.3 and
+    R = 300 (explicit); gamma 1.3, factor 2 and adaptive-CFL exponents (0.5, 2.0) (implicit):
+    the reference's own runs against the oracle."""
+    ref, info = G.load(case)
+    O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
+    if info["mode"] == "explicit":
+        hist = O.explicit_run(info["steps"])
+        refh = ref["residual_history"].reshape(-1, 10)
+        tol = TOL
+    else:
+        hist = O.implicit_run(info["steps"])[:, :12]
+        refh = ref["implicit_history"].reshape(-1, 12)
+        tol = 1e-10
+    assert np.max(np.abs(hist - refh) / np.maximum(np.abs(refh), 1e-300)) <= tol
+    assert rel_err(O.get_state(), ref["final_state"]) <= tol
+
+
 @pytest.mark.parametrize("case", G.CASES_2D_IMPLICIT)
 def test_2d_implicit_history_matches_reference(case):
     """The reference's own 2-D implicit steps (triangles, 4x4 blocks) against the oracle's
