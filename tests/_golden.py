@@ -22,11 +22,11 @@ CASES = ["explicit_bump_local", "explicit_bump_global", "explicit_gauss_pitch",
 # triangle meshes (the reference's 2-D path); the fixtures pad per-cell data to the 3-D
 # layout: five conserved variables (rho w = 0) and four face slots (the fourth -1)
 CASES_2D = ["explicit_bump2d_local"]
-# the reference's 2-D implicit run (its 4x4-block systems solved through the linear-solver
+# the reference's 2-D implicit runs (their 4x4-block systems solved through the linear-solver
 # facade as 5x5 blocks with a decoupled spanwise-momentum row)
-CASES_2D_IMPLICIT = ["implicit_bump2d_ilu0"]
+CASES_2D_IMPLICIT = ["implicit_bump2d_ilu0", "implicit_bump2d_jacobi_global"]
 # implicit histories only (no operator dumps): the oracle against the reference's own steps
-CASES_IMPLICIT_HISTORY = ["implicit_bump_global", "implicit_gauss_pitch"]
+CASES_IMPLICIT_HISTORY = ["implicit_bump_global", "implicit_gauss_pitch", "implicit_bump_ramp"]
 # the rest of the option surface (stage coefficients, limiter and Harten constants, gas
 # constants, adaptive-CFL exponents), histories only
 CASES_OPTIONS = ["explicit_bump_options", "implicit_bump_options"]

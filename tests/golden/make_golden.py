@@ -80,6 +80,17 @@ CASES = {
                                   mach=meshgen.freestream_mach_vector(0.7, 3.0, -2.0),
                                   smoother="ILU0", lin_tol=1e-2, lin_maxiter=300),
                              8, "implicit", False),
+    "implicit_bump_ramp": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),
+                           dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
+                                mach=(0.7, 0, 0), smoother="ILU0", lin_tol=1e-2,
+                                lin_maxiter=300, fs_ramp=5, fs_frac=0.3),
+                           8, "implicit", False),
+    "implicit_bump2d_jacobi_global": (lambda: meshgen.bump_channel_2d(24, 8, 0.08),
+                                      dict(solver="IMPLICIT", local="NO", cfl=10.0,
+                                           cfl_max=1000.0, mach=(0.6, 0.04, 0),
+                                           smoother="DAMPED_JACOBI", lin_tol=1e-2,
+                                           lin_maxiter=300),
+                                      8, "implicit", False),
     # the rest of the option surface on the path: `besi` lines added to the case file, `oracle`
     # the matching keyword arguments of the CPU restatement
     "explicit_bump_options": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),

@@ -93,9 +93,9 @@ def test_implicit_history_matches_reference(case):
 
 
 @pytest.mark.parametrize("case", G.CASES_IMPLICIT_HISTORY)
-def test_implicit_history_matches_reference_global_dt_and_pitch(case):
-    """Implicit steps with a global time step, and on the pitched Gaussian box (block ILU(0)
-    in the reference's cell order), against the reference's own runs."""
+def test_implicit_history_matches_reference_more_cases(case):
+    """Implicit steps with a global time step, on the pitched Gaussian box (block ILU(0) in
+    the reference's cell order) and with a freestream ramp, against the reference's own runs."""
     ref, info = G.load(case)
     O = pyoracle.Oracle(G.mesh_of(info), **G.oracle_kwargs(info))
     hist = O.implicit_run(info["steps"])
@@ -125,9 +125,10 @@ def test_option_surface_matches_reference(case):
 
 @pytest.mark.parametrize("case", G.CASES_2D_IMPLICIT)
 def test_2d_implicit_history_matches_reference(case):
-    """The reference's own 2-D implicit steps (triangles, 4x4 blocks) against the oracle's
-    2-D restatement: the reference adds every Jacobian block once per conserved variable
-    (Q9), four times in 2-D, which is the default count; five, the 3-D count, does not match."""
+    """The reference's own 2-D implicit steps (triangles, 4x4 blocks; block ILU(0) with local
+    time steps, block Jacobi with a global one) against the oracle's 2-D restatement: the
+    reference adds every Jacobian block once per conserved variable (Q9), four times in 2-D,
+    which is the default count; five, the 3-D count, does not match."""
     ref, info = G.load(case)
     refh = ref["implicit_history"].reshape(-1, 12)
     kw = G.oracle_kwargs(info)
