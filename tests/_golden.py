@@ -13,6 +13,7 @@ MESHES = {
     "bump_channel_12x4x4_h0.08": lambda: meshgen.bump_channel(12, 4, 4, 0.08),
     "gaussian_box_8x4x8_r1.05": lambda: meshgen.gaussian_box(8, 4, 8),
     "bump_channel_2d_24x8_h0.08": lambda: meshgen.bump_channel_2d(24, 8, 0.08),
+    "bump_channel_24x8x6_h0.04": lambda: meshgen.bump_channel(24, 8, 6, 0.04),
 }
 
 CASES = ["explicit_bump_local", "explicit_bump_global", "explicit_gauss_pitch",

@@ -91,6 +91,14 @@ CASES = {
                                            smoother="DAMPED_JACOBI", lin_tol=1e-2,
                                            lin_maxiter=300),
                                       8, "implicit", False),
+    # the reference's own converged state: a 4 % bump at Mach 0.5 solved by its implicit solver
+    # (adaptive CFL 10 -> 1000) for 200 steps, where its residual has fallen to the rounding
+    # floor (about 4e-12 of the first)
+    "implicit_bump_converged": (lambda: meshgen.bump_channel(24, 8, 6, 0.04),
+                                dict(solver="IMPLICIT", local="YES", cfl=10.0, cfl_max=1000.0,
+                                     mach=(0.5, 0, 0), smoother="ILU0", lin_tol=1e-2,
+                                     lin_maxiter=300),
+                                200, "implicit", False),
     # the rest of the option surface on the path: `besi` lines added to the case file, `oracle`
     # the matching keyword arguments of the CPU restatement
     "explicit_bump_options": (lambda: meshgen.bump_channel(12, 4, 4, 0.08),

@@ -104,6 +104,42 @@ def test_implicit_history_matches_reference_more_cases(case):
     assert rel_err(O.get_state(), ref["final_state"]) <= 1e-10
 
 
+def test_converged_state_and_forces_match_reference():
+    """The converged gate against the reference itself: the reference's implicit solver run
+    for 200 steps on the 4 % bump at Mach 0.5 (adaptive CFL, residual at its rounding floor)
+    against the oracle driven to a 1e-10 drop along the path the library's converged-state
+    tests take (CFL ramp 10 -> 1000 over 10 steps): states within 1e-10 (max norm, relative)
+    and slip-wall force coefficients within 1e-10.  The GPU's converged states are checked
+    against the oracle's in tests/test_gpu_converged.py."""
+    import os
+    ref, info = G.load("implicit_bump_converged")
+    mesh = G.mesh_of(info)
+    mach = tuple(info["meta"]["mach"])
+    O = pyoracle.Oracle(mesh, solver=1, local_dt=1, cfl=10.0, mach=mach, lin_precond=1,
+                        lin_tol=1e-2, lin_maxiter=300, lin_restart=30, ramp_steps=10,
+                        ramp_cfl0=10.0, ramp_cfl1=1000.0, threads=os.cpu_count() or 1)
+    res = lambda h: float(np.sqrt(np.sum(h[14:19] ** 2)))
+    r0 = None
+    for _ in range(60):
+        h = O.implicit_run(5)
+        r0 = res(h[0]) if r0 is None else r0
+        if res(h[-1]) <= 1e-10 * r0:
+            break
+    assert res(h[-1]) <= 1e-10 * r0
+    U = O.get_state()
+    Uref = ref["final_state"].reshape(U.shape)
+    assert np.abs(U - Uref).max() / np.abs(Uref).max() <= 1e-10
+    g = O.geometry()
+    wall = g["face_type"] == 1
+
+    def coeff(S):
+        u = S[g["face_owner"][wall]]
+        p = 0.4 * (u[:, 4] - 0.5 * (u[:, 1] ** 2 + u[:, 2] ** 2 + u[:, 3] ** 2) / u[:, 0])
+        return (p[:, None] * g["face_S"][wall]).sum(axis=0) / (0.5 * sum(m * m for m in mach))
+
+    assert np.abs(coeff(U) - coeff(Uref)).max() <= 1e-10
+
+
 @pytest.mark.parametrize("case", G.CASES_OPTIONS)
 def test_option_surface_matches_reference(case):
     """Three stage coefficients, Venkatakrishnan factor 2, Harten limit 0.2, gamma 1.3 and
