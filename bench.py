@@ -106,7 +106,7 @@ WORKLOADS = {
                                 train=(1, 32), test=(2, 8), data_iters=1500, eval_iters=1500,
                                 train_steps=3000, batch=8192,
                                 opts=dict(solver_type=0, local_time_step=1, courant_num=0.8)),
-    # learned warm start at the survey's configuration 4: the Gaussian-bump box at 60x30x60
+    # learned warm start at full size: the Gaussian-bump box at 60x30x60
     # hexes (648,000 tets); training data = 512 conditions (seed 1) solved to a 1e-8 drop by the
     # batched implicit sweep (FP32 system with 16-bit storage, linear tolerance prod_tol); the
     # network trained for 20,000 AdamW steps (lr 1e-3) on the converged ones; 64 held-out

@@ -58,7 +58,7 @@ def test_max_over_ranks_with_two_gloo_ranks():
 
 
 def test_reference_arm_under_torchrun_prints_one_line():
-    """Launched as the driver launches N ranks, only rank 0 runs the reference arm and prints."""
+    """Launched by torchrun with N ranks, only rank 0 runs the reference arm and prints."""
     import socket
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))

@@ -4,7 +4,7 @@ driven to the same drop, and the oracle's slip-wall force against bes_wall_force
 The reference logs no force coefficients; they are defined as the slip-wall CSV does
 (src/SolutionSnapshot.cpp:268-309): the owner cell's pressure times the dimensional face
 normal, summed over the slip-wall faces, over the dynamic pressure 1/2 rho |M|^2 with rho = 1
-and a reference area of 1.  Tolerances (the benchmark spec's converged gate): states 1e-8 relative
+and a reference area of 1.  Tolerances (the converged-state gate): states 1e-8 relative
 (max norm over all cells and variables), force coefficients 1e-8 absolute.
 
 Also here: the implicit path with a freestream ramp (FREESTREAM_RAMP, src/Config.cpp:688-706)

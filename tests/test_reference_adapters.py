@@ -2,7 +2,7 @@
 with bes_gb300 behind its operator and solver classes.
 
 Needs the reference checkout (environment variable BES_REFERENCE_DIR): the adapters compile
-against its headers and link with its sources.  Without a GPU the driver builds the
+against its headers and link with its sources.  Without a GPU bes_driver builds the
 reference's objects from the .besi file and stops, with the reference's error convention,
 where the library reports that no CUDA device is present; with one, --operators compares the
 GPU adapters with the reference's GradientGreenGauss, LimiterVenkatakrishnan and
