@@ -743,7 +743,7 @@ def _physical(U, gamma=1.4):
 
 
 def run_production(args, wl, torch, mesh, clocks):
-    """Learned warm start (configuration 4): training data from the batched implicit sweep,
+    """Learned warm start on the Gaussian-bump box: training data from the batched implicit sweep,
     AdamW training of the FiLM MLP on the GPU, held-out conditions solved from the prediction
     and from the freestream (batched), the plain FP64 solver on a sample; value: cell-updates/s
     of the warm-started sweep."""
