@@ -216,6 +216,8 @@ SAVE_INTERVAL = 10
     assert o.venkatakrishnan_factor == 5.0 and o.harten_correction_limit == 0.05
     assert o.gas_constant == 287.0 and o.specific_heat_ratio == 1.4
     assert o.precision == 0
+    # 0: each Jacobian block added once per conserved variable of the mesh, as the reference
+    assert o.jacobian_repeat == 0
 
 
 @pytest.mark.parametrize("word,value", [("FP64", 0), ("MIXED", 1), ("MIXED_PACKED", 2)])
